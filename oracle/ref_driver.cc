@@ -1,0 +1,154 @@
+// Test-infrastructure driver for the UNMODIFIED reference (zilliztech/pyglass).
+//
+// This file is ours; it only #includes the reference's header-only sources where they lie
+// (include path given by oracle/Makefile) and re-exports the pieces the parity suite needs as a
+// plain C ABI, so that Python (ctypes) can run the reference searcher, quantizers and graph
+// builders on the same inputs as the GPU path.  It is never linked into the product.
+//
+// Reference entry points wrapped here:
+//   glass::create_searcher            glass/searcher/graph_searcher.hpp:256-391
+//   GraphSearcherBase::SetData/Search/SearchBatch/SetEf/GetLastSearchAvgDistCmps
+//                                      glass/searcher/searcher_base.hpp:7-19
+//   glass::create_hnsw / create_nsg    glass/hnsw/hnsw.hpp:74-133, glass/nsg/nsg.hpp:411-434
+//   Graph<int>::load/save             glass/graph.hpp:106-153
+//   Quantizer train/add/get_computer   glass/quant/*.hpp
+#include <omp.h>
+
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "glass/hnsw/hnsw.hpp"
+#include "glass/nsg/nsg.hpp"
+#include "glass/searcher/graph_searcher.hpp"
+
+namespace {
+
+struct RefSearcher {
+    std::unique_ptr<glass::GraphSearcherBase> s;
+};
+
+// Runs `fn` with a freshly trained quantizer of the requested kind.
+template <typename Fn>
+int with_quant(const std::string &quant, const std::string &metric, int d, Fn &&fn) {
+    using glass::Metric;
+    bool l2 = metric != "IP";
+    if (quant == "SQ8U") {
+        if (l2) { glass::SQ8QuantizerUniform<Metric::L2> q(d); return fn(q); }
+        glass::SQ8QuantizerUniform<Metric::IP> q(d); return fn(q);
+    }
+    if (quant == "SQ4U") {
+        if (l2) { glass::SQ4QuantizerUniform<Metric::L2> q(d); return fn(q); }
+        glass::SQ4QuantizerUniform<Metric::IP> q(d); return fn(q);
+    }
+    if (quant == "E5M2") {
+        if (l2) { glass::E5M2Quantizer<Metric::L2> q(d); return fn(q); }
+        glass::E5M2Quantizer<Metric::IP> q(d); return fn(q);
+    }
+    if (quant == "FP32") {
+        if (l2) { glass::FP32Quantizer<Metric::L2> q(d); return fn(q); }
+        glass::FP32Quantizer<Metric::IP> q(d); return fn(q);
+    }
+    return -1;
+}
+
+template <typename Q>
+void calib_params(const Q &q, float *params) {
+    params[0] = params[1] = 0.0f;
+    if constexpr (requires { q.calibrator.dif; }) {
+        params[0] = q.calibrator.min;
+        params[1] = q.calibrator.dif;
+    } else if constexpr (requires { q.calibrator.max; }) {
+        params[0] = q.calibrator.max;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void ref_set_num_threads(int n) { omp_set_num_threads(n); }
+
+// Builds a graph with the reference CPU builder and saves it in the glass format.
+double ref_build_graph(const char *index_type, const float *data, int n, int d, const char *metric,
+                       const char *quant, int R, int L, const char *out_path) {
+    std::unique_ptr<glass::Builder> b;
+    std::string t(index_type);
+    if (t == "HNSW") b = glass::create_hnsw(metric, quant, R, L);
+    else if (t == "NSG") b = glass::create_nsg(quant, R, L, false);
+    else if (t == "SSG") b = glass::create_nsg(quant, R, L, true);
+    if (!b) return -1.0;
+    auto g = b->Build(data, n, d);
+    g.save(out_path);
+    return b->GetConstructionTime();
+}
+
+void *ref_searcher_create(const char *graph_path, const float *data, int n, int d, const char *metric,
+                          const char *quant, const char *refine) {
+    glass::Graph<int> g;
+    g.load(graph_path, "glass");
+    auto *r = new RefSearcher;
+    r->s = glass::create_searcher(std::move(g), metric, quant, refine);
+    if (!r->s) { delete r; return nullptr; }
+    r->s->SetData(data, n, d);
+    return r;
+}
+
+void ref_searcher_set_ef(void *h, int ef) { ((RefSearcher *)h)->s->SetEf(ef); }
+
+void ref_searcher_search(void *h, const float *q, int k, int *ids, float *dis) {
+    ((RefSearcher *)h)->s->Search(q, k, ids, dis);
+}
+
+void ref_searcher_search_batch(void *h, const float *qs, int nq, int k, int *ids, float *dis) {
+    ((RefSearcher *)h)->s->SearchBatch(qs, nq, k, ids, dis);
+}
+
+double ref_searcher_dist_cmps(void *h) { return ((RefSearcher *)h)->s->GetLastSearchAvgDistCmps(); }
+
+void ref_searcher_destroy(void *h) { delete (RefSearcher *)h; }
+
+// Code size in bytes of one encoded row for quantizer `quant` at dimension d.
+int ref_code_size(const char *quant, const char *metric, int d) {
+    return with_quant(quant, metric, d, [](auto &q) { return (int)q.code_size(); });
+}
+
+// Trains the quantizer on data[n*d] exactly as SetData does, writes all n codes (n*code_size bytes)
+// and the calibrator parameters (min,dif for affine; max for symmetric).
+int ref_encode(const char *quant, const char *metric, const float *data, int n, int d, char *codes,
+               float *params) {
+    return with_quant(quant, metric, d, [&](auto &q) {
+        q.train(data, n);
+        q.add(data, n);
+        for (int i = 0; i < n; ++i) std::memcpy(codes + (int64_t)i * q.code_size(), q.get_code(i), q.code_size());
+        calib_params(q, params);
+        return 0;
+    });
+}
+
+// Trains on data like SetData, then evaluates the per-query distance computer of `quant` for
+// every (query, id) pair: out[qi*m + j] = computer_qi(ids[qi*m + j]).  Also returns the encoded
+// query rows (the computer's private query buffer, code_size bytes each; float queries for
+// E5M2/FP32 are returned as their dim_align*4 bytes).
+int ref_query_distances(const char *quant, const char *metric, const float *data, int n, int d,
+                        const float *queries, int nq, const int *ids, int m, double *out, char *qcodes,
+                        int qcode_stride) {
+    return with_quant(quant, metric, d, [&](auto &q) {
+        q.train(data, n);
+        q.add(data, n);
+        for (int qi = 0; qi < nq; ++qi) {
+            auto comp = q.get_computer(queries + (int64_t)qi * d);
+            for (int j = 0; j < m; ++j) out[(int64_t)qi * m + j] = (double)comp(ids[(int64_t)qi * m + j]);
+            if (qcodes) {
+                using X = typename std::decay_t<decltype(comp)>::X;
+                int nbytes = (int)(q.dim_align() * sizeof(X));
+                if constexpr (sizeof(X) == 1) nbytes = q.code_size();
+                std::memcpy(qcodes + (int64_t)qi * qcode_stride, comp.q, std::min(nbytes, qcode_stride));
+            }
+        }
+        return 0;
+    });
+}
+
+}  // extern "C"
