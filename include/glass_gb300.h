@@ -1,0 +1,139 @@
+/*
+ * glass_gb300.h - C ABI of the GB300 graph-search path (libglass_gb300.so).
+ *
+ * Plain pointers, sizes and status codes; no C++ or framework types cross this boundary.  Every
+ * entry point returns GSX_OK (0) or a GSX_ERR_* code; gsx_last_error() gives the message of the
+ * calling thread's last failure.  Each declaration names the reference interface it replaces
+ * (zilliztech/pyglass, path:line).
+ *
+ * Threading: a searcher handle owns one CUDA stream and its device buffers; calls on the same
+ * handle must not overlap (the reference's Searcher.search is not re-entrant either,
+ * glass/searcher/graph_searcher.hpp:133).  Different handles may be used from different threads.
+ */
+#ifndef GLASS_GB300_H
+#define GLASS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GSX_OK = 0,
+    GSX_ERR_INVALID = 1,     /* bad argument, unknown string, malformed file */
+    GSX_ERR_CUDA = 2,        /* CUDA runtime error (message carries the CUDA error string) */
+    GSX_ERR_NOMEM = 3,       /* device or host allocation failed / admission refused */
+    GSX_ERR_STATE = 4,       /* call out of order (e.g. search before set_data) */
+    GSX_ERR_IO = 5,          /* file could not be opened / read / written */
+    GSX_ERR_TIMEOUT = 6,     /* a bounded wait gave up */
+    GSX_ERR_UNSUPPORTED = 7  /* valid in the reference but outside this path (e.g. PQ8) */
+};
+
+typedef struct gsx_graph gsx_graph;
+typedef struct gsx_searcher gsx_searcher;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *gsx_last_error(void);
+/* Library version string. */
+const char *gsx_version(void);
+/* Number of visible CUDA devices (0 when there is none; never fails). */
+int gsx_device_count(void);
+
+/* ---- graphs: glass::Graph<int32_t> (glass/graph.hpp:26-246) -------------------------------- */
+
+/* Graph(filename, format) / Graph::load (python/bindings.cc:47-57, glass/graph.hpp:255-287).
+ * format: "glass" (with optional HNSW upper levels, HNSWInitializer.hpp:64-75), "nsg",
+ * "diskann" or "hnswlib" (graph.hpp:289-379).  The graph is validated: every id is -1 or in
+ * [0, N), and every HNSW upper-level neighbour exists on that level. */
+int gsx_graph_load(const char *filename, const char *format, gsx_graph **out);
+/* Builds a graph from memory: adj is N*K int32 (-1 padded), eps the entry points. */
+int gsx_graph_create(const int32_t *adj, int32_t N, int32_t K, const int32_t *eps, int32_t nep, gsx_graph **out);
+/* Graph::save (graph.hpp:240-253) in the glass format. */
+int gsx_graph_save(const gsx_graph *g, const char *filename);
+/* N, K, number of entry points, and whether HNSW upper levels are present. */
+int gsx_graph_info(const gsx_graph *g, int32_t *N, int32_t *K, int32_t *nep, int32_t *has_hnsw);
+/* Copies the adjacency (N*K int32) out. */
+int gsx_graph_adjacency(const gsx_graph *g, int32_t *adj_out);
+void gsx_graph_destroy(gsx_graph *g);
+
+/* ---- searchers: GraphSearcherBase (glass/searcher/searcher_base.hpp:7-19) ---------------- */
+
+/* create_searcher(graph, metric, quantizer, refine_quant) (graph_searcher.hpp:256-391).
+ * metric "L2" | "IP"; quantizer "SQ8U" | "SQ4U" | "E5M2" | "FP32" (an unknown name selects
+ * FP32, as the reference's quantizer_map does); refine_quant "" or "FP32" (Refiner with
+ * get_refine_factor, graph_searcher.hpp:227-254).  The graph's contents move into the searcher
+ * (python/bindings.cc:98); *graph is left empty but must still be destroyed.  device = CUDA
+ * ordinal. */
+int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quantizer, const char *refine_quant,
+                        int device, gsx_searcher **out);
+void gsx_searcher_destroy(gsx_searcher *s);
+
+/* SetData (graph_searcher.hpp:51-70, refiner.hpp:26-37): calibrates the quantizer, encodes the
+ * n x dim fp32 rows on the device and keeps the codes (and the FP32 refine store) resident. */
+int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t dim);
+
+/* SetEf / GetEf (graph_searcher.hpp:72-74). */
+int gsx_searcher_set_ef(gsx_searcher *s, int32_t ef);
+int gsx_searcher_get_ef(const gsx_searcher *s, int32_t *ef);
+
+/* Search (graph_searcher.hpp:131-138, refiner.hpp:45-70): one query, host buffers; ids[k],
+ * dis[k].  The plain per-query GPU form: one launch, one warp. */
+int gsx_searcher_search(gsx_searcher *s, const float *query, int32_t k, int32_t *ids, float *dis);
+
+/* SearchBatch (graph_searcher.hpp:143-159, refiner.hpp:72-90): nq queries from host memory,
+ * results to host memory, one batched launch.  dis may be NULL. */
+int gsx_searcher_search_batch(gsx_searcher *s, const float *queries, int32_t nq, int32_t k, int32_t *ids,
+                              float *dis);
+
+/* Batched search with per-query ef and k (either array may be NULL = uniform), buffers in
+ * DEVICE memory, enqueued on `stream` (cudaStream_t, NULL = the searcher's stream) without a
+ * host synchronisation.  Output rows have stride kmax = max k.  cmps (may be NULL) receives
+ * per-query distance counts.  No reference counterpart: the batched/persistent form. */
+int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
+                                     const int32_t *d_ef, const int32_t *d_k, int32_t kmax, int32_t *d_ids,
+                                     float *d_dis, int32_t *d_cmps, void *stream);
+
+/* Same as above with HOST buffers (copies inside), synchronous. */
+int gsx_searcher_search_batch_mixed(gsx_searcher *s, const float *queries, int32_t nq, int32_t k,
+                                    const int32_t *ef, const int32_t *kq, int32_t kmax, int32_t *ids, float *dis);
+
+/* Optimize (graph_searcher.hpp:76-129): the reference tunes CPU prefetch depth on 1,000
+ * sampled base rows; here the same sample tunes warps per CTA, visited-table size and lanes
+ * per row.  num_threads is accepted for signature parity and ignored. */
+int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads);
+
+/* GetLastSearchAvgDistCmps (graph_searcher.hpp:140-141): average distance computations per
+ * query of the last batched search. */
+int gsx_searcher_get_last_search_avg_dist_cmps(const gsx_searcher *s, double *out);
+
+/* Tuning knobs chosen by gsx_searcher_optimize (0 = automatic). */
+typedef struct {
+    int32_t warps_per_block;  /* queries per CTA */
+    int32_t table_bits;       /* log2 of the per-query visited-table slots in shared memory */
+    int32_t lanes_per_row;    /* lanes cooperating on one code row (SQ kinds) */
+    int32_t prefetch;         /* L2 prefetch of adjacency rows of accepted candidates */
+} gsx_tuning;
+int gsx_searcher_get_tuning(const gsx_searcher *s, gsx_tuning *t);
+int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t);
+
+/* Device memory (bytes) the index holds resident, and the bytes one in-flight query needs. */
+int gsx_searcher_memory(const gsx_searcher *s, size_t *index_bytes, size_t *per_query_bytes);
+
+/* ---- distance computers: ComputerImpl::operator() (glass/quant/computer.hpp:42-75) -------- */
+
+/* out[i*m+j] = distance(query i, base row ids[i*m+j]) with the searcher's quantizer (refine=0)
+ * or its FP32 refine store (refine=1), computed by the same device code the search uses.
+ * Host buffers.  SQ distances are exact integers returned as double. */
+int gsx_searcher_distances(gsx_searcher *s, const float *queries, int32_t nq, const int32_t *ids, int32_t m,
+                           int32_t refine, double *out);
+
+/* Copies out the encoded base rows (n*code_size bytes) and calibrator parameters (2 floats). */
+int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int32_t *code_size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLASS_GB300_H */

@@ -1,0 +1,75 @@
+// Device-side encoding of base rows (SetData's quant.add, glass/searcher/graph_searcher.hpp:51-58):
+// SQ8U (sq8u_quant.hpp:242-254), SQ4U (sq4u_quant.hpp:311-329), E5M2 (e5m2_quant.hpp:382-394) and
+// the zero-padded FP32 rows of FP32Quantizer / the refine store (fp32_quant.hpp:428-440).
+// The arithmetic is the query encoder's (gsx_device.cuh), so base and query codes agree with
+// the reference bit for bit.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gsx_device.cuh"
+#include "gsx_internal.h"
+
+namespace gsx {
+
+namespace {
+
+template <int KIND, int METRIC>
+__global__ void encode_rows(const float *__restrict__ data, int64_t n, int d, int csize, float p0, float p1,
+                            uint32_t *__restrict__ out) {
+    const int nw = csize >> 2;
+    const int64_t total = n * (int64_t)nw;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = t / nw;
+        const int wi = (int)(t - row * nw);
+        const float *x = data + row * (int64_t)d;
+        uint32_t word = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int b = 4 * wi + k;
+            uint32_t byte;
+            if (KIND == K_E5M2) byte = b < d ? e5m2_of(x[b]) : 0u;
+            else byte = sq_code_byte<KIND, METRIC>(x, d, b, p0, p1);
+            word |= byte << (8 * k);
+        }
+        out[t] = word;
+    }
+}
+
+__global__ void pad_rows(const float *__restrict__ data, int64_t n, int d, int dalign, float *__restrict__ out) {
+    const int64_t total = n * (int64_t)dalign;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = t / dalign;
+        const int j = (int)(t - row * dalign);
+        out[t] = j < d ? data[row * (int64_t)d + j] : 0.0f;
+    }
+}
+
+int grid_for(int64_t work) {
+    int64_t g = (work + 255) / 256;
+    if (g > 152 * 32) g = 152 * 32;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, int d, int dalign, int csize, float p0,
+                          float p1, uint8_t *out, cudaStream_t st) {
+    (void)dalign;
+    const int g = grid_for(n * (csize >> 2));
+    uint32_t *o = reinterpret_cast<uint32_t *>(out);
+    if (kind == K_SQ4U) encode_rows<K_SQ4U, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
+    else if (kind == K_SQ8U && metric == M_IP) encode_rows<K_SQ8U, M_IP><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
+    else if (kind == K_SQ8U) encode_rows<K_SQ8U, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
+    else if (kind == K_E5M2) encode_rows<K_E5M2, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pad_rows(const float *data, int64_t n, int d, int dalign, float *out, cudaStream_t st) {
+    pad_rows<<<grid_for(n * dalign), 256, 0, st>>>(data, n, d, dalign, out);
+    return cudaGetLastError();
+}
+
+}  // namespace gsx

@@ -1,0 +1,681 @@
+// The C ABI of libglass_gb300 (include/glass_gb300.h): GraphSearcherBase
+// (glass/searcher/searcher_base.hpp:7-19) and create_searcher (graph_searcher.hpp:256-391) over
+// the device kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "gsx_host.h"
+
+namespace gsx {
+
+namespace {
+thread_local std::string g_err;
+}
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    cudaGetLastError();  // clear a sticky launch error of this thread
+    return fail(e == cudaErrorMemoryAllocation ? GSX_ERR_NOMEM : GSX_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int DevBuf::ensure(size_t n) {
+    if (n <= bytes && p) return GSX_OK;
+    release();
+    size_t want = n < 256 ? 256 : n;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    bytes = want;
+    return GSX_OK;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+namespace {
+
+// quantizer_map (glass/quant/quant.hpp:25-43); operator[] on an unknown key yields FP32.
+int parse_quant(const std::string &q, int *kind) {
+    static const char *unsupported[] = {"FP16", "BF16", "SQ8", "SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "SQ2U", "PQ8"};
+    if (q == "SQ8U") *kind = K_SQ8U;
+    else if (q == "SQ4U") *kind = K_SQ4U;
+    else if (q == "E5M2") *kind = K_E5M2;
+    else {
+        for (const char *u : unsupported)
+            if (q == u) return fail(GSX_ERR_UNSUPPORTED, "quantizer %s is outside the GPU search path", u);
+        *kind = K_FP32;
+    }
+    return GSX_OK;
+}
+
+int layout(int kind, int d, int *dalign, int *csize) {
+    int align = 16, nbits = 32;
+    if (kind == K_SQ8U) { align = 64; nbits = 8; }
+    else if (kind == K_SQ4U) { align = 128; nbits = 4; }
+    else if (kind == K_E5M2) { align = 16; nbits = 8; }
+    *dalign = (d + align - 1) / align * align;  // tensor.hpp:122-123
+    *csize = *dalign * nbits / 8;
+    return GSX_OK;
+}
+
+// r-th smallest of v (0-based), on a private copy.
+float kth(std::vector<float> &v, int64_t r) {
+    std::nth_element(v.begin(), v.begin() + r, v.end());
+    return v[(size_t)r];
+}
+
+// Calibrator training (calibrator.hpp:481-514, quant/utils.hpp:584-603, sq8u_quant.hpp:240,
+// sq4u_quant.hpp:307-309).  find_minmax keeps the top = int64(nitems*ratio)+1 smallest / largest
+// values; the result is the top-th smallest and top-th largest.
+void calibrate(int kind, int metric, const float *data, int64_t n, int d, float *p) {
+    p[0] = p[1] = 0.0f;
+    if (kind == K_SQ8U) {
+        const int64_t nitems = n * d;
+        if (metric == M_L2) {
+            float mn = data[0], mx = data[0];
+            for (int64_t i = 1; i < nitems; ++i) {
+                mn = data[i] < mn ? data[i] : mn;
+                mx = data[i] > mx ? data[i] : mx;
+            }
+            p[0] = mn;
+            p[1] = mx - mn;
+        } else {
+            float mx = 0.0f;
+            for (int64_t i = 0; i < nitems; ++i) mx = std::fabs(data[i]) > mx ? std::fabs(data[i]) : mx;
+            p[0] = mx;
+        }
+    } else if (kind == K_SQ4U) {
+        int64_t nitems = (int64_t)((float)(n * (int64_t)d) * 0.1f);
+        if (nitems < 1) nitems = 1;
+        int64_t top = (int64_t)((float)nitems * 0.01f) + 1;
+        if (top > nitems) top = nitems;
+        std::vector<float> v(data, data + nitems);
+        const float mn = kth(v, top - 1);
+        const float mx = kth(v, nitems - top);
+        p[0] = mn;
+        p[1] = mx - mn;
+    }
+}
+
+int set_device(const gsx_searcher *s) {
+    GSX_CUDA(cudaSetDevice(s->device));
+    return GSX_OK;
+}
+
+template <typename T>
+int upload(DevBuf &b, const T *src, size_t n, cudaStream_t st) {
+    int rc = b.ensure(n * sizeof(T));
+    if (rc) return rc;
+    if (n) GSX_CUDA(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
+    return GSX_OK;
+}
+
+int default_table_bits(const gsx_searcher *s, int efmax) {
+    // expected visits ~ ef * K; keep the table at most about half full
+    int64_t want = (int64_t)efmax * s->ix.K + 64;
+    int bits = kMinTableBits;
+    while ((1ll << bits) < want && bits < 30) ++bits;
+    return bits;
+}
+
+int kin_of(const gsx_searcher *s, int k) {
+    const int rk = s->has_refine ? (int)((float)k * s->refine_factor) : k;
+    return rk;
+}
+
+// Prepares a launch configuration for a batch whose largest k/ef are kmax/efmax.
+int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int table_bits_override, LaunchCfg *cfg) {
+    const int cap = std::max(kin_of(s, kmax), efmax);
+    if (cap > kMaxCap) return fail(GSX_ERR_UNSUPPORTED, "pool capacity %d (k, ef) exceeds %d", cap, kMaxCap);
+    int bits = table_bits_override > 0 ? table_bits_override
+               : (s->tuning.table_bits > 0 ? s->tuning.table_bits : default_table_bits(s, efmax));
+    int wpb = single ? 1 : (s->tuning.warps_per_block > 0 ? s->tuning.warps_per_block : 4);
+    int lpr = s->tuning.lanes_per_row > 0 ? s->tuning.lanes_per_row
+              : ((s->kind == K_E5M2 || s->kind == K_FP32) ? 4 : (s->ix.csize > 256 ? 4 : 1));
+    WarpLayout L;
+    // shrink the table (down to the minimum) until one warp's slice fits; beyond that the
+    // global-memory table path is used
+    while (!make_layout(s->ix, cap, bits, s->tuning.prefetch, &L) && bits > kMinTableBits) --bits;
+    if (!make_layout(s->ix, cap, bits, s->tuning.prefetch, &L))
+        return fail(GSX_ERR_UNSUPPORTED, "per-query state does not fit in shared memory");
+    while (wpb > 1 && (size_t)wpb * L.total > 227 * 1024) wpb >>= 1;
+    cfg->warps_per_block = wpb;
+    cfg->lanes_per_row = lpr;
+    cfg->L = L;
+    int per_sm = search_max_blocks_per_sm(s->ix, *cfg);
+    if (per_sm < 1) per_sm = 1;
+    const int want = (nq + wpb - 1) / wpb;
+    cfg->blocks = std::max(1, std::min(want, per_sm * s->num_sms));
+    return GSX_OK;
+}
+
+// Enqueues one batch on `st`; nothing is synchronised.
+int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int32_t *d_ef, const int32_t *d_k,
+            int kmax, int efmax, int32_t *d_ids, float *d_dis, int32_t *d_cmps, bool single, cudaStream_t st,
+            const LaunchCfg *cfg_in = nullptr) {
+    if (nq <= 0) return GSX_OK;
+    LaunchCfg cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else {
+        int rc = make_cfg(s, kmax, efmax, nq, single, 0, &cfg);
+        if (rc) return rc;
+    }
+    int rc = s->status.ensure((size_t)nq * 4);
+    if (rc) return rc;
+    if ((rc = s->counters.ensure(256))) return rc;
+    GSX_CUDA(cudaMemsetAsync(s->counters.p, 0, 8, st));
+    BatchView bv{};
+    bv.queries = d_q;
+    bv.nq = nq;
+    bv.k = k;
+    bv.ef = ef;
+    bv.k_per = d_k;
+    bv.ef_per = d_ef;
+    bv.order = nullptr;
+    bv.single = single ? 1 : 0;
+    bv.out_stride = kmax;
+    bv.out_ids = d_ids;
+    bv.out_dis = d_dis;
+    bv.cmps = d_cmps;
+    bv.status = s->status.as<int32_t>();
+    bv.counter = s->counters.as<unsigned>();
+    bv.overflow = s->counters.as<unsigned>() + 1;
+    GSX_CUDA(launch_search(s->ix, bv, cfg, st));
+    return GSX_OK;
+}
+
+// Re-runs the queries whose visited table overflowed with a global-memory table large enough
+// for every node of the graph (exact for any ef), then patches their results in place.
+int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int32_t *d_ef,
+                     const int32_t *d_k, int kmax, int efmax, int32_t *d_ids, float *d_dis, int32_t *d_cmps,
+                     bool single, cudaStream_t st) {
+    unsigned nover = 0;
+    GSX_CUDA(cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaStreamSynchronize(st));
+    if (nover == 0) return GSX_OK;
+    s->h_status.resize((size_t)nq);
+    GSX_CUDA(cudaMemcpyAsync(s->h_status.data(), s->status.p, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaStreamSynchronize(st));
+    std::vector<int32_t> redo;
+    for (int i = 0; i < nq; ++i)
+        if (s->h_status[i]) redo.push_back(i);
+    int gbits = 12;
+    while ((1ll << gbits) < 2ll * s->ix.N + 2 * kMaxDegree && gbits < 28) ++gbits;
+    LaunchCfg cfg;
+    int rc = make_cfg(s, kmax, efmax, (int)redo.size(), single, kMinTableBits, &cfg);
+    if (rc) return rc;
+    cfg.L.table_bits = 0;
+    cfg.warps_per_block = 4;
+    const int slots_max = 64;
+    cfg.blocks = std::max(1, std::min(((int)redo.size() + 3) / 4, slots_max / 4));
+    const size_t slots = (size_t)cfg.blocks * cfg.warps_per_block;
+    if ((rc = s->gtab.ensure(slots * ((size_t)1 << gbits) * 4))) return rc;
+    if ((rc = upload(s->order, redo.data(), redo.size(), st))) return rc;
+    if ((rc = s->status.ensure((size_t)nq * 4))) return rc;
+    GSX_CUDA(cudaMemsetAsync(s->counters.p, 0, 8, st));
+    BatchView bv{};
+    bv.queries = d_q;
+    bv.nq = (int)redo.size();
+    bv.k = k;
+    bv.ef = ef;
+    bv.k_per = d_k;
+    bv.ef_per = d_ef;
+    bv.order = s->order.as<int32_t>();
+    bv.single = single ? 1 : 0;
+    bv.out_stride = kmax;
+    bv.out_ids = d_ids;
+    bv.out_dis = d_dis;
+    bv.cmps = d_cmps;
+    bv.status = s->status.as<int32_t>();
+    bv.counter = s->counters.as<unsigned>();
+    bv.overflow = s->counters.as<unsigned>() + 1;
+    bv.gtab = s->gtab.as<int32_t>();
+    bv.gtab_bits = gbits;
+    GSX_CUDA(launch_search(s->ix, bv, cfg, st));
+    GSX_CUDA(cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaStreamSynchronize(st));
+    if (nover) return fail(GSX_ERR_STATE, "visited table overflow persisted for %u queries", nover);
+    return GSX_OK;
+}
+
+// Host-buffer batch: copies in, searches, resolves overflows, copies out, synchronises.
+int host_batch(gsx_searcher *s, const float *queries, int nq, int k, const int32_t *ef_per, const int32_t *k_per,
+               int kmax, int32_t *ids, float *dis, bool single) {
+    if (!s->has_data) return fail(GSX_ERR_STATE, "search before set_data");
+    if (nq < 0 || k <= 0 || kmax < k) return fail(GSX_ERR_INVALID, "bad nq/k (nq=%d k=%d kmax=%d)", nq, k, kmax);
+    if (nq == 0) return GSX_OK;
+    int rc = set_device(s);
+    if (rc) return rc;
+    cudaStream_t st = s->stream;
+    const int d = s->ix.d;
+    int efmax = s->ef;
+    if (ef_per) {
+        efmax = 1;
+        for (int i = 0; i < nq; ++i) {
+            if (ef_per[i] <= 0) return fail(GSX_ERR_INVALID, "ef must be positive");
+            efmax = std::max(efmax, ef_per[i]);
+        }
+    }
+    if (k_per)
+        for (int i = 0; i < nq; ++i)
+            if (k_per[i] <= 0 || k_per[i] > kmax) return fail(GSX_ERR_INVALID, "per-query k out of range");
+    if ((rc = upload(s->q, queries, (size_t)nq * d, st))) return rc;
+    if ((rc = s->ids.ensure((size_t)nq * kmax * 4))) return rc;
+    if ((rc = s->dis.ensure((size_t)nq * kmax * 4))) return rc;
+    if ((rc = s->cmps.ensure((size_t)nq * 4))) return rc;
+    const int32_t *d_ef = nullptr, *d_k = nullptr;
+    if (ef_per) {
+        if ((rc = upload(s->efp, ef_per, (size_t)nq, st))) return rc;
+        d_ef = s->efp.as<int32_t>();
+    }
+    if (k_per) {
+        if ((rc = upload(s->kp, k_per, (size_t)nq, st))) return rc;
+        d_k = s->kp.as<int32_t>();
+    }
+    rc = enqueue(s, s->q.as<float>(), nq, k, s->ef, d_ef, d_k, kmax, efmax, s->ids.as<int32_t>(), s->dis.as<float>(),
+                 s->cmps.as<int32_t>(), single, st);
+    if (rc) return rc;
+    rc = resolve_overflow(s, s->q.as<float>(), nq, k, s->ef, d_ef, d_k, kmax, efmax, s->ids.as<int32_t>(),
+                          s->dis.as<float>(), s->cmps.as<int32_t>(), single, st);
+    if (rc) return rc;
+    GSX_CUDA(cudaMemcpyAsync(ids, s->ids.p, (size_t)nq * kmax * 4, cudaMemcpyDeviceToHost, st));
+    if (dis) GSX_CUDA(cudaMemcpyAsync(dis, s->dis.p, (size_t)nq * kmax * 4, cudaMemcpyDeviceToHost, st));
+    s->h_cmps.resize((size_t)nq);
+    GSX_CUDA(cudaMemcpyAsync(s->h_cmps.data(), s->cmps.p, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaStreamSynchronize(st));
+    if (!single) {
+        // SearchBatch: average distance computations (graph_searcher.hpp:156-158)
+        int64_t tot = 0;
+        for (int i = 0; i < nq; ++i) tot += s->h_cmps[i];
+        s->last_avg_cmps = (double)tot / nq;
+    }
+    return GSX_OK;
+}
+
+}  // namespace
+
+}  // namespace gsx
+
+using namespace gsx;
+
+extern "C" {
+
+const char *gsx_last_error(void) { return g_err.c_str(); }
+
+const char *gsx_version(void) { return "glass-gb300 0.1.0 (sm_103a)"; }
+
+int gsx_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int gsx_graph_load(const char *filename, const char *format, gsx_graph **out) {
+    if (!filename || !out) return fail(GSX_ERR_INVALID, "null argument");
+    auto *g = new gsx_graph;
+    int rc = graph_load(filename, format, g->g);
+    if (rc) {
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return GSX_OK;
+}
+
+int gsx_graph_create(const int32_t *adj, int32_t N, int32_t K, const int32_t *eps, int32_t nep, gsx_graph **out) {
+    if (!adj || !out || N <= 0 || K <= 0 || nep < 0 || (nep && !eps)) return fail(GSX_ERR_INVALID, "bad graph arguments");
+    auto *g = new gsx_graph;
+    g->g.N = N;
+    g->g.K = K;
+    g->g.adj.assign(adj, adj + (size_t)N * K);
+    g->g.eps.assign(eps, eps + nep);
+    int rc = validate_graph(g->g);
+    if (rc) {
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return GSX_OK;
+}
+
+int gsx_graph_save(const gsx_graph *g, const char *filename) {
+    if (!g || !filename) return fail(GSX_ERR_INVALID, "null argument");
+    if (g->g.N == 0) return fail(GSX_ERR_STATE, "graph is empty (moved into a searcher?)");
+    return graph_save(g->g, filename);
+}
+
+int gsx_graph_info(const gsx_graph *g, int32_t *N, int32_t *K, int32_t *nep, int32_t *has_hnsw) {
+    if (!g) return fail(GSX_ERR_INVALID, "null graph");
+    if (N) *N = g->g.N;
+    if (K) *K = g->g.K;
+    if (nep) *nep = (int32_t)g->g.eps.size();
+    if (has_hnsw) *has_hnsw = g->g.has_hnsw;
+    return GSX_OK;
+}
+
+int gsx_graph_adjacency(const gsx_graph *g, int32_t *adj_out) {
+    if (!g || !adj_out) return fail(GSX_ERR_INVALID, "null argument");
+    std::memcpy(adj_out, g->g.adj.data(), g->g.adj.size() * 4);
+    return GSX_OK;
+}
+
+void gsx_graph_destroy(gsx_graph *g) { delete g; }
+
+int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quantizer, const char *refine_quant,
+                        int device, gsx_searcher **out) {
+    if (!graph || !out) return fail(GSX_ERR_INVALID, "null argument");
+    if (graph->g.N == 0) return fail(GSX_ERR_STATE, "graph is empty (already moved into a searcher?)");
+    int ndev = gsx_device_count();
+    if (ndev == 0) return fail(GSX_ERR_CUDA, "no CUDA device is visible");
+    if (device < 0 || device >= ndev) return fail(GSX_ERR_INVALID, "device %d out of range", device);
+    int kind;
+    int rc = parse_quant(quantizer ? quantizer : "", &kind);
+    if (rc) return rc;
+    const std::string rq = refine_quant ? refine_quant : "";
+    int rkind = K_FP32;
+    if (!rq.empty() && (rc = parse_quant(rq, &rkind))) return rc;
+    if (!rq.empty() && rkind != K_FP32)
+        return fail(GSX_ERR_UNSUPPORTED, "refine quantizer %s is outside the GPU search path", rq.c_str());
+    auto *s = new gsx_searcher;
+    s->kind = kind;
+    // metric_map (common.hpp:13-19): unknown names fall on the default-constructed L2
+    s->metric = (metric && std::string(metric) == "IP") ? M_IP : M_L2;
+    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ4U, 1.0 otherwise (in which
+    // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
+    const float factor = (kind == K_SQ8U || kind == K_SQ4U) ? 1.5f : 1.0f;
+    s->has_refine = (!rq.empty() && factor != 1.0f) ? 1 : 0;
+    s->refine_factor = factor;
+    s->device = device;
+    s->graph = std::move(graph->g);  // the Python Graph is moved from (python/bindings.cc:98)
+    graph->g = HostGraph();
+    auto bad = [&](int code) {
+        gsx_searcher_destroy(s);
+        return code;
+    };
+    if ((rc = set_device(s))) return bad(rc);
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bad(cuda_fail(e, "cudaStreamCreate"));
+    cudaEventCreate(&s->ev0);
+    cudaEventCreate(&s->ev1);
+    cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device);
+    const HostGraph &g = s->graph;
+    if ((rc = upload(s->adj, g.adj.data(), g.adj.size(), s->stream))) return bad(rc);
+    if ((rc = upload(s->eps, g.eps.data(), g.eps.size(), s->stream))) return bad(rc);
+    if (g.has_hnsw) {
+        if ((rc = upload(s->levels, g.levels.data(), g.levels.size(), s->stream))) return bad(rc);
+        if ((rc = upload(s->loff, g.loff.data(), g.loff.size(), s->stream))) return bad(rc);
+        if ((rc = upload(s->lists, g.lists.data(), std::max<size_t>(g.lists.size(), 1), s->stream))) return bad(rc);
+    }
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return bad(cuda_fail(e, "graph upload"));
+    IndexView &ix = s->ix;
+    ix.N = g.N;
+    ix.K = g.K;
+    ix.adj = s->adj.as<int32_t>();
+    ix.nep = (int32_t)g.eps.size();
+    ix.eps = s->eps.as<int32_t>();
+    ix.has_hnsw = g.has_hnsw;
+    ix.hK = g.hK;
+    ix.hep = g.hep;
+    ix.levels = s->levels.as<int32_t>();
+    ix.loff = s->loff.as<int64_t>();
+    ix.lists = s->lists.as<int32_t>();
+    ix.kind = kind;
+    ix.metric = s->metric;
+    ix.has_refine = s->has_refine;
+    ix.refine_factor = factor;
+    *out = s;
+    return GSX_OK;
+}
+
+void gsx_searcher_destroy(gsx_searcher *s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->q, &s->ids,
+                      &s->dis, &s->status, &s->cmps, &s->efp, &s->kp, &s->order, &s->counters, &s->gtab,
+                      &s->dist_out, &s->dist_ids})
+        b->release();
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t dim) {
+    if (!s || !data) return fail(GSX_ERR_INVALID, "null argument");
+    if (dim <= 0 || n <= 0) return fail(GSX_ERR_INVALID, "bad data shape %d x %d", n, dim);
+    if (n < s->ix.N) return fail(GSX_ERR_INVALID, "data has %d rows but the graph has %d nodes", n, s->ix.N);
+    int rc = set_device(s);
+    if (rc) return rc;
+    IndexView &ix = s->ix;
+    ix.d = dim;
+    layout(s->kind, dim, &ix.dalign, &ix.csize);
+    float p[2];
+    calibrate(s->kind, s->metric, data, n, dim, p);
+    ix.p0 = p[0];
+    ix.p1 = p[1];
+    cudaStream_t st = s->stream;
+    DevBuf raw;
+    if ((rc = upload(raw, data, (size_t)n * dim, st))) return rc;
+    if ((rc = s->codes.ensure((size_t)n * ix.csize))) return rc;
+    if (s->kind == K_FP32) {
+        GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.dalign, s->codes.as<float>(), st));
+    } else {
+        GSX_CUDA(launch_encode(s->kind, s->metric, raw.as<float>(), n, dim, ix.dalign, ix.csize, ix.p0, ix.p1,
+                               s->codes.as<uint8_t>(), st));
+    }
+    if (s->has_refine) {
+        ix.r_dalign = (dim + 15) / 16 * 16;
+        if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 4))) return rc;
+        GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.r_dalign, s->r_codes.as<float>(), st));
+    }
+    GSX_CUDA(cudaStreamSynchronize(st));
+    ix.codes = s->codes.as<uint8_t>();
+    ix.r_codes = s->r_codes.as<float>();
+    // keep 1,000 sampled rows for optimize (graph_searcher.hpp:62-69)
+    s->sample_n = std::min(1000, n);
+    std::mt19937 rng(12345);
+    s->sample.resize((size_t)s->sample_n * dim);
+    for (int i = 0; i < s->sample_n; ++i) {
+        const int r = (int)(rng() % (uint32_t)n);
+        std::memcpy(&s->sample[(size_t)i * dim], data + (size_t)r * dim, (size_t)dim * 4);
+    }
+    s->has_data = true;
+    return GSX_OK;
+}
+
+int gsx_searcher_set_ef(gsx_searcher *s, int32_t ef) {
+    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+    if (ef <= 0) return fail(GSX_ERR_INVALID, "ef must be positive");
+    s->ef = ef;
+    return GSX_OK;
+}
+
+int gsx_searcher_get_ef(const gsx_searcher *s, int32_t *ef) {
+    if (!s || !ef) return fail(GSX_ERR_INVALID, "null argument");
+    *ef = s->ef;
+    return GSX_OK;
+}
+
+int gsx_searcher_search(gsx_searcher *s, const float *query, int32_t k, int32_t *ids, float *dis) {
+    if (!s || !query || !ids) return fail(GSX_ERR_INVALID, "null argument");
+    return host_batch(s, query, 1, k, nullptr, nullptr, k, ids, dis, true);
+}
+
+int gsx_searcher_search_batch(gsx_searcher *s, const float *queries, int32_t nq, int32_t k, int32_t *ids, float *dis) {
+    if (!s || (nq > 0 && (!queries || !ids))) return fail(GSX_ERR_INVALID, "null argument");
+    return host_batch(s, queries, nq, k, nullptr, nullptr, k, ids, dis, false);
+}
+
+int gsx_searcher_search_batch_mixed(gsx_searcher *s, const float *queries, int32_t nq, int32_t k, const int32_t *ef,
+                                    const int32_t *kq, int32_t kmax, int32_t *ids, float *dis) {
+    if (!s || (nq > 0 && (!queries || !ids))) return fail(GSX_ERR_INVALID, "null argument");
+    if (kq && kmax <= 0) return fail(GSX_ERR_INVALID, "kmax required with per-query k");
+    if (!kq) kmax = k;
+    return host_batch(s, queries, nq, k, ef, kq, kmax, ids, dis, false);
+}
+
+int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
+                                     const int32_t *d_ef, const int32_t *d_k, int32_t kmax, int32_t *d_ids,
+                                     float *d_dis, int32_t *d_cmps, void *stream) {
+    if (!s || (nq > 0 && (!d_queries || !d_ids))) return fail(GSX_ERR_INVALID, "null argument");
+    if (!s->has_data) return fail(GSX_ERR_STATE, "search before set_data");
+    if (k <= 0) return fail(GSX_ERR_INVALID, "k must be positive");
+    if (kmax < k) kmax = k;
+    int rc = set_device(s);
+    if (rc) return rc;
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    // with per-query ef on the device the caller's searcher ef is the upper bound
+    return enqueue(s, d_queries, nq, k, s->ef, d_ef, d_k, kmax, s->ef, d_ids, d_dis, d_cmps, false, st);
+}
+
+int gsx_searcher_get_last_search_avg_dist_cmps(const gsx_searcher *s, double *out) {
+    if (!s || !out) return fail(GSX_ERR_INVALID, "null argument");
+    *out = s->last_avg_cmps;
+    return GSX_OK;
+}
+
+int gsx_searcher_get_tuning(const gsx_searcher *s, gsx_tuning *t) {
+    if (!s || !t) return fail(GSX_ERR_INVALID, "null argument");
+    *t = s->tuning;
+    return GSX_OK;
+}
+
+int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
+    if (!s || !t) return fail(GSX_ERR_INVALID, "null argument");
+    if (t->warps_per_block < 0 || t->warps_per_block > 8 || (t->warps_per_block & (t->warps_per_block - 1)))
+        return fail(GSX_ERR_INVALID, "warps_per_block must be 0 or a power of two <= 8");
+    if (t->lanes_per_row != 0 && t->lanes_per_row != 1 && t->lanes_per_row != 2 && t->lanes_per_row != 4)
+        return fail(GSX_ERR_INVALID, "lanes_per_row must be 0, 1, 2 or 4");
+    if (t->table_bits != 0 && (t->table_bits < kMinTableBits || t->table_bits > 16))
+        return fail(GSX_ERR_INVALID, "table_bits must be 0 or in [%d, 16]", kMinTableBits);
+    s->tuning = *t;
+    if ((s->kind == K_E5M2 || s->kind == K_FP32) && s->tuning.lanes_per_row == 2) s->tuning.lanes_per_row = 4;
+    return GSX_OK;
+}
+
+int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
+    (void)num_threads;
+    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+    if (!s->has_data) return fail(GSX_ERR_STATE, "optimize before set_data");
+    int rc = set_device(s);
+    if (rc) return rc;
+    const int nq = s->sample_n, k = 10, d = s->ix.d;
+    cudaStream_t st = s->stream;
+    if ((rc = upload(s->q, s->sample.data(), (size_t)nq * d, st))) return rc;
+    if ((rc = s->ids.ensure((size_t)nq * k * 4))) return rc;
+    if ((rc = s->dis.ensure((size_t)nq * k * 4))) return rc;
+    const gsx_tuning saved = s->tuning;
+    const int base_bits = default_table_bits(s, std::max(s->ef, kin_of(s, k)));
+    std::vector<int> lprs = (s->kind == K_E5M2 || s->kind == K_FP32) ? std::vector<int>{1, 4} : std::vector<int>{1, 2, 4};
+    gsx_tuning best = saved;
+    float best_ms = 1e30f;
+    for (int wpb : {2, 4, 8})
+        for (int lpr : lprs)
+            for (int db : {-1, 0, 1}) {
+                gsx_tuning t{wpb, std::max(kMinTableBits, base_bits + db), lpr, saved.prefetch};
+                s->tuning = t;
+                float ms_min = 1e30f;
+                bool ok = true;
+                for (int rep = 0; rep < 3 && ok; ++rep) {
+                    cudaEventRecord(s->ev0, st);
+                    rc = enqueue(s, s->q.as<float>(), nq, k, s->ef, nullptr, nullptr, k, s->ef, s->ids.as<int32_t>(),
+                                 s->dis.as<float>(), nullptr, false, st);
+                    if (rc) { ok = false; break; }
+                    cudaEventRecord(s->ev1, st);
+                    unsigned nover = 0;
+                    cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st);
+                    if (cudaStreamSynchronize(st) != cudaSuccess) {
+                        s->tuning = saved;
+                        return cuda_fail(cudaGetLastError(), "optimize");
+                    }
+                    if (nover) { ok = false; break; }  // a table that overflows is not a candidate
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+                    ms_min = std::min(ms_min, ms);
+                }
+                if (ok && ms_min < best_ms) {
+                    best_ms = ms_min;
+                    best = t;
+                }
+            }
+    s->tuning = best;
+    return GSX_OK;
+}
+
+int gsx_searcher_memory(const gsx_searcher *s, size_t *index_bytes, size_t *per_query_bytes) {
+    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+    if (index_bytes)
+        *index_bytes = s->adj.bytes + s->eps.bytes + s->levels.bytes + s->loff.bytes + s->lists.bytes + s->codes.bytes +
+                       s->r_codes.bytes;
+    if (per_query_bytes) {
+        // device bytes one in-flight query holds outside the resident index: its fp32 row,
+        // outputs (k up to 256), status and counter
+        *per_query_bytes = (size_t)s->ix.d * 4 + 256 * 8 + 16;
+    }
+    return GSX_OK;
+}
+
+int gsx_searcher_distances(gsx_searcher *s, const float *queries, int32_t nq, const int32_t *ids, int32_t m,
+                           int32_t refine, double *out) {
+    if (!s || !queries || !ids || !out) return fail(GSX_ERR_INVALID, "null argument");
+    if (!s->has_data) return fail(GSX_ERR_STATE, "distances before set_data");
+    if (refine && !s->has_refine) return fail(GSX_ERR_STATE, "searcher has no refine store");
+    for (int64_t i = 0; i < (int64_t)nq * m; ++i)
+        if (ids[i] < 0 || ids[i] >= s->ix.N) return fail(GSX_ERR_INVALID, "id %d out of range", ids[i]);
+    int rc = set_device(s);
+    if (rc) return rc;
+    cudaStream_t st = s->stream;
+    if ((rc = upload(s->q, queries, (size_t)nq * s->ix.d, st))) return rc;
+    if ((rc = upload(s->dist_ids, ids, (size_t)nq * m, st))) return rc;
+    if ((rc = s->dist_out.ensure((size_t)nq * m * 8))) return rc;
+    GSX_CUDA(launch_distances(s->ix, refine, s->q.as<float>(), nq, s->dist_ids.as<int32_t>(), m,
+                              s->dist_out.as<double>(), st));
+    GSX_CUDA(cudaMemcpyAsync(out, s->dist_out.p, (size_t)nq * m * 8, cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaStreamSynchronize(st));
+    return GSX_OK;
+}
+
+int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int32_t *code_size) {
+    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+    if (!s->has_data) return fail(GSX_ERR_STATE, "codes before set_data");
+    if (code_size) *code_size = s->ix.csize;
+    if (params) {
+        params[0] = s->ix.p0;
+        params[1] = s->ix.p1;
+    }
+    if (codes) {
+        int rc = set_device(s);
+        if (rc) return rc;
+        GSX_CUDA(cudaMemcpy(codes, s->codes.p, (size_t)s->ix.N * s->ix.csize, cudaMemcpyDeviceToHost));
+    }
+    return GSX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// Host-side runtime of libglass_gb300: graphs, searchers, errors.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/glass_gb300.h"
+#include "gsx_internal.h"
+
+namespace gsx {
+
+// Records the calling thread's error message and returns `code`.
+int fail(int code, const char *fmt, ...);
+// Maps a CUDA error to GSX_ERR_CUDA / GSX_ERR_NOMEM with a message.
+int cuda_fail(cudaError_t e, const char *what);
+
+#define GSX_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return ::gsx::cuda_fail(e_, #call); \
+    } while (0)
+
+struct HostGraph {
+    int32_t N = 0, K = 0;
+    std::vector<int32_t> adj;
+    std::vector<int32_t> eps;
+    int32_t has_hnsw = 0, hK = 0, hep = 0;
+    std::vector<int32_t> levels;
+    std::vector<int64_t> loff;
+    std::vector<int32_t> lists;
+};
+
+int graph_load(const char *path, const char *format, HostGraph &g);
+int graph_save(const HostGraph &g, const char *path);
+int validate_graph(const HostGraph &g);
+
+// A device allocation that grows on demand.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);
+    void release();
+    ~DevBuf() { release(); }
+    template <typename T>
+    T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+}  // namespace gsx
+
+// The opaque handles of the C ABI.
+struct gsx_graph {
+    gsx::HostGraph g;
+};
+
+struct gsx_searcher {
+    // create_searcher arguments
+    int kind = gsx::K_FP32, metric = gsx::M_L2;
+    int has_refine = 0;
+    float refine_factor = 1.0f;
+    int device = 0;
+    int ef = 32;
+    gsx::HostGraph graph;  // host copy kept for save/inspection
+
+    // device index
+    bool has_data = false;
+    gsx::IndexView ix{};
+    gsx::DevBuf adj, eps, levels, loff, lists, codes, r_codes;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+
+    // per-call scratch (device)
+    gsx::DevBuf q, ids, dis, status, cmps, efp, kp, order, counters, gtab, dist_out, dist_ids;
+    // host copies for reporting
+    std::vector<int32_t> h_cmps, h_status;
+    double last_avg_cmps = 0.0;
+
+    // sample of base rows kept for optimize (graph_searcher.hpp:62-69)
+    std::vector<float> sample;
+    int32_t sample_n = 0;
+
+    gsx_tuning tuning{0, 0, 0, 1};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};

@@ -1,0 +1,88 @@
+// Internal types shared by the host runtime (gsx_api.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace gsx {
+
+// Quantizer kinds and metrics (values follow glass/quant/quant.hpp:25-43 and glass/common.hpp).
+enum Kind : int { K_FP32 = 0, K_E5M2 = 3, K_SQ8U = 4, K_SQ4U = 7 };
+enum MetricId : int { M_L2 = 0, M_IP = 1 };
+
+constexpr int kMaxDegree = 64;       // graph degree handled per row (two 32-wide chunks)
+constexpr int kMaxCap = 1024;        // largest pool capacity max(k*factor, ef)
+constexpr int kMinTableBits = 7;     // smallest visited table: 128 slots
+
+// Device-resident index, as the kernels see it.
+struct IndexView {
+    int32_t N, K;
+    const int32_t *adj;       // N*K, -1 padded (glass/graph.hpp:26-104)
+    int32_t nep;
+    const int32_t *eps;
+    int32_t has_hnsw, hK, hep;
+    const int32_t *levels;    // N
+    const int64_t *loff;      // N+1 offsets into lists
+    const int32_t *lists;     // upper-level lists, levels[u]*hK per node (HNSWInitializer.hpp:64-75)
+    int32_t kind, metric, d, dalign, csize;
+    float p0, p1;             // calibrator (min, dif) or (max, 0)
+    const uint8_t *codes;     // N*csize
+    int32_t has_refine;
+    float refine_factor;
+    int32_t r_dalign;
+    const float *r_codes;     // N*r_dalign fp32 rows
+};
+
+// One batched launch.
+struct BatchView {
+    const float *queries;     // nq*d fp32
+    int32_t nq;
+    int32_t k, ef;            // uniform values
+    const int32_t *k_per;     // optional per-query k
+    const int32_t *ef_per;    // optional per-query ef
+    const int32_t *order;     // optional work order (a permutation of 0..nq-1)
+    int32_t single;           // Searcher.search semantics: expansion limit max(k, ef)
+    int32_t out_stride;
+    int32_t *out_ids;
+    float *out_dis;
+    int32_t *cmps;            // optional per-query distance counts
+    int32_t *status;          // per-query: 0 ok, 1 visited table full (query left unanswered)
+    unsigned int *counter;    // work-queue head, zeroed before the launch
+    unsigned int *overflow;   // number of overflowed queries
+    int32_t *gtab;            // optional global visited tables, one slot per warp
+    int32_t gtab_bits;
+};
+
+// Byte offsets of one warp's slice of dynamic shared memory.
+struct WarpLayout {
+    int pool_key, pool_id, cand_id, cand_key, acc_ub, acc_key, acc_id, fq, qc, table;
+    int total;                // bytes per warp (multiple of 16)
+    int cap;                  // pool capacity available
+    int fq_len;               // floats in the fp32 query buffer
+    int table_bits;           // 0 => visited table in global memory (BatchView::gtab)
+    int prefetch;
+};
+
+struct LaunchCfg {
+    int warps_per_block;
+    int lanes_per_row;
+    int blocks;
+    WarpLayout L;
+};
+
+// Computes the per-warp layout; returns false if it cannot fit in shared memory.
+bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, WarpLayout *L);
+
+// Kernel launchers (search_kernel.cu).  Return cudaGetLastError() of the launch.
+cudaError_t launch_search(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st);
+int search_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg);
+
+// Encoding and distance kernels (encode_kernel.cu).
+cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, int d, int dalign, int csize, float p0,
+                          float p1, uint8_t *out, cudaStream_t st);
+cudaError_t launch_pad_rows(const float *data, int64_t n, int d, int dalign, float *out, cudaStream_t st);
+cudaError_t launch_distances(const IndexView &ix, int refine, const float *queries, int nq, const int32_t *ids,
+                             int m, double *out, cudaStream_t st);
+
+}  // namespace gsx

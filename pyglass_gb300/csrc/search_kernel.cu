@@ -1,0 +1,641 @@
+// Warp-per-query beam search over a fixed-degree graph: the GPU form of GraphSearcher
+// (glass/searcher/graph_searcher.hpp:131-224) with LinearPool/Bitset (glass/neighbor.hpp:31-79,
+// 320-433), the HNSW upper-level descent (glass/hnsw/HNSWInitializer.hpp:41-62) and the FP32
+// Refiner tail (glass/searcher/refiner.hpp:45-110) fused after the traversal.
+//
+// One warp owns one query at a time and takes the next query from a device work queue
+// (persistent kernel).  Per expansion the warp
+//   1. finds the first unexpanded pool entry (ballot over the pool),
+//   2. reads the adjacency row with one coalesced load (lane i <- neighbour i),
+//   3. drops repeats inside the row (match.any) and visited ids (shared-memory hash table,
+//      atomicCAS), keeping row order,
+//   4. computes the distances of the new neighbours, a team of LPR lanes per row,
+//   5. merges them into the sorted pool.
+// The merge places every candidate exactly where the reference's sequential insert would
+// (upper-bound position, earlier inserts first among equal distances, truncation at capacity),
+// so on equal distances the pool, the expansion order, the distance count and the result are
+// those of the CPU searcher.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gsx_device.cuh"
+#include "gsx_internal.h"
+
+namespace gsx {
+
+namespace {
+
+constexpr int32_t kChecked = (int32_t)0x80000000;
+constexpr int32_t kIdMask = 0x7fffffff;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Visited set: open addressing with linear probing over 2^bits int32 slots (-1 = empty).
+// Returns true if v was absent (and is now present).  Probing is bounded by the table size; the
+// caller keeps the load under 3/4 so a free slot always exists.
+__device__ __forceinline__ bool visit(int32_t *tab, int bits, int32_t v) {
+    const uint32_t mask = (1u << bits) - 1u;
+    uint32_t h = ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
+    for (uint32_t p = 0; p <= mask; ++p) {
+        int32_t old = atomicCAS(tab + h, -1, v);
+        if (old == -1) return true;
+        if (old == v) return false;
+        h = (h + 1u) & mask;
+    }
+    return false;
+}
+
+// First index in [lo, hi) whose entry is not yet expanded, or hi.
+__device__ __forceinline__ int first_unchecked(const int32_t *pid, int lo, int hi, int lane) {
+    for (int base = lo; base < hi; base += 32) {
+        int i = base + lane;
+        bool un = i < hi && pid[i] >= 0;
+        unsigned b = __ballot_sync(kFull, un);
+        if (b) return base + __ffs(b) - 1;
+    }
+    return hi;
+}
+
+__device__ __forceinline__ int upper_bound_u32(const uint32_t *a, int n, uint32_t x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] > x) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int count_le_i32(const int32_t *a, int n, int x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] > x) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+struct WarpState {
+    uint32_t *pkey;
+    int32_t *pid;
+    int32_t *cand_id;
+    uint32_t *cand_key;
+    int32_t *acc_ub;
+    uint32_t *acc_key;
+    int32_t *acc_id;
+    float *fq;
+    uint32_t *qc;
+    int32_t *tab;
+    int tbits;
+};
+
+// Merges candidates cand_{id,key}[0..m) (in insertion order, m <= 64) into the pool
+// pkey/pid[0..S) of capacity cap.  Exactly the state LinearPool::insert (neighbor.hpp:382-396)
+// reaches by inserting them one after the other: a candidate lands after every pool entry with
+// an equal or smaller key and after the earlier candidates with equal keys; entries pushed past
+// cap are dropped.  `lb` is a lower bound of the first unexpanded index and is updated.
+__device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, int m, int lane) {
+    int nacc = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int j = lane + 32 * h;
+        const bool valid = j < m;
+        uint32_t kj = valid ? w.cand_key[j] : 0u;
+        int acc = 0, ub = 0, rank = 0;
+        if (valid) {
+            bool reject = (S == cap) && kj >= w.pkey[S - 1];
+            if (!reject) {
+                for (int i = 0; i < m; ++i) {
+                    uint32_t ki = w.cand_key[i];
+                    rank += (ki < kj) || (ki == kj && i < j);
+                }
+                ub = upper_bound_u32(w.pkey, S, kj);
+                acc = (ub + rank) < cap;
+            }
+        }
+        if (acc) {
+            w.acc_ub[rank] = ub;
+            w.acc_key[rank] = kj;
+            w.acc_id[rank] = w.cand_id[j];
+        }
+        nacc += __popc(__ballot_sync(kFull, acc));
+        if (m <= 32) break;
+    }
+    __syncwarp();
+    if (nacc == 0) return;
+    const int lo = w.acc_ub[0];
+    // shift pool entries [lo, S) to their new places, highest chunk first (no entry is read
+    // after its slot was written: destinations are >= sources and strictly increasing)
+    for (int top = S; top > lo; top -= 32) {
+        const int i = top - 1 - lane;
+        const bool act = i >= lo;
+        uint32_t k = 0;
+        int32_t id = 0;
+        int np = 0;
+        if (act) {
+            k = w.pkey[i];
+            id = w.pid[i];
+            np = i + count_le_i32(w.acc_ub, nacc, i);
+        }
+        __syncwarp();
+        if (act && np < cap) {
+            w.pkey[np] = k;
+            w.pid[np] = id;
+        }
+        __syncwarp();
+    }
+    for (int r = lane; r < nacc; r += 32) {
+        const int p = w.acc_ub[r] + r;
+        w.pkey[p] = w.acc_key[r];
+        w.pid[p] = w.acc_id[r];
+    }
+    const int sl = count_le_i32(w.acc_ub, nacc, lb);
+    const int nl = lb + sl;
+    lb = lo < nl ? lo : nl;
+    S = (S + m) < cap ? (S + m) : cap;
+    __syncwarp();
+}
+
+// Distances of cand_id[0..m) -> cand_key[0..m).
+template <int KIND, int METRIC, int LPR>
+__device__ __forceinline__ void compute_dists(const IndexView &ix, WarpState &w, int m, int32_t qsq, int lane) {
+    constexpr int TEAMS = 32 / LPR;
+    const int team = lane / LPR, sub = lane % LPR;
+    for (int b = 0; b < m; b += TEAMS) {
+        const int j = b + team;
+        const bool act = j < m;
+        const int id = act ? w.cand_id[j] : 0;
+        uint32_t key;
+        if (IsIntKind<KIND>::value) {
+            int32_t part = act ? sq_partial<KIND, METRIC, LPR>(ix.codes, ix.csize, id, sub, w.qc) : 0;
+            key = key_of(sq_finish<KIND, METRIC, LPR>(part, qsq));
+        } else {
+            const uint8_t *row = ix.codes + (size_t)id * (size_t)ix.csize;
+            float dv = float_dist<KIND == K_E5M2, METRIC, LPR>(row, ix.dalign >> 4, sub, w.fq, act);
+            key = key_of(dv);
+        }
+        if (act && sub == 0) w.cand_key[j] = key;
+    }
+    __syncwarp();
+}
+
+// FP32 refine distance of cand_id[0..m) into cand_key (as float bits), 4 lanes per row.
+template <int METRIC>
+__device__ __forceinline__ void refine_dists(const IndexView &ix, const int32_t *ids, float *out, int m,
+                                             const float *fq, int lane) {
+    const int team = lane >> 2, sub = lane & 3;
+    for (int b = 0; b < m; b += 8) {
+        const int j = b + team;
+        const bool act = j < m;
+        const int id = act ? ids[j] : 0;
+        const uint8_t *row = reinterpret_cast<const uint8_t *>(ix.r_codes + (size_t)id * (size_t)ix.r_dalign);
+        float dv = float_dist<false, METRIC, 4>(row, ix.r_dalign >> 4, sub, fq, act);
+        if (act && sub == 0) out[j] = dv;
+    }
+    __syncwarp();
+}
+
+// Encodes the query held in w.fq into w.qc (SQ kinds); returns the sum of squared codes.
+template <int KIND, int METRIC>
+__device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState &w, int lane) {
+    if (!IsIntKind<KIND>::value) return 0;
+    const int nw = ix.csize >> 2;
+    int32_t sq = 0;
+    for (int wi = lane; wi < nw; wi += 32) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            word |= sq_code_byte<KIND, METRIC>(w.fq, ix.d, 4 * wi + t, ix.p0, ix.p1) << (8 * t);
+        if (KIND == K_SQ4U) {
+            uint32_t lo = word & 0x0F0F0F0Fu, hi = (word >> 4) & 0x0F0F0F0Fu;
+            w.qc[wi] = lo;
+            w.qc[nw + wi] = hi;
+            sq = __dp4a(lo, lo, (uint32_t)sq);
+            sq = __dp4a(hi, hi, (uint32_t)sq);
+        } else {
+            w.qc[wi] = word;
+            sq = __dp4a(word, word, (uint32_t)sq);
+        }
+    }
+    sq = team_sum<32>(sq);
+    __syncwarp();
+    return sq;
+}
+
+template <int KIND, int METRIC, int LPR>
+__device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpLayout &L, WarpState &w, int qi,
+                           int lane) {
+    const int kq = bv.k_per ? bv.k_per[qi] : bv.k;
+    const int efq = bv.ef_per ? bv.ef_per[qi] : bv.ef;
+    // Refiner: reorder_k = (int)(k * factor) (refiner.hpp:46, 73)
+    const int rk = ix.has_refine ? (int)((float)kq * ix.refine_factor) : kq;
+    const bool refine = ix.has_refine && rk != kq;
+    const int kin = refine ? rk : kq;
+    int cap = kin > efq ? kin : efq;
+    if (cap > L.cap) cap = L.cap;  // host sizes L.cap >= every query's capacity
+    // SearchBatch: pool.reset(nb, ef, max(k, ef)); Search: pool.reset(nb, max(k,ef), max(k,ef))
+    const int ef_expand = bv.single ? cap : efq;
+
+    // query -> shared memory (fp32, zero padded), then the quantizer's encoding
+    const float *q = bv.queries + (size_t)qi * (size_t)ix.d;
+    for (int j = lane; j < L.fq_len; j += 32) w.fq[j] = j < ix.d ? __ldg(q + j) : 0.0f;
+    __syncwarp();
+    const int32_t qsq = prepare_query<KIND, METRIC>(ix, w, lane);
+
+    // visited table reset
+    const int tsize = 1 << w.tbits;
+    for (int j = lane * 4; j < tsize; j += 128) *reinterpret_cast<int4 *>(w.tab + j) = make_int4(-1, -1, -1, -1);
+    __syncwarp();
+    const int tlimit = (tsize >> 2) * 3;
+
+    int S = 0, lb = 0, nvis = 0, cmps = 0;
+    bool overflow = false;
+
+    // ---- initialize_search (graph.hpp:229-238) ----
+    if (ix.has_hnsw) {
+        // HNSWInitializer::initialize (HNSWInitializer.hpp:41-62): greedy descent; within a pass
+        // the list of the node held at the start of the pass is scanned and the running best
+        // (strictly smaller distance) kept, i.e. the first minimum of the list.
+        int u = ix.hep;
+        if (lane == 0) w.cand_id[0] = u;
+        __syncwarp();
+        compute_dists<KIND, METRIC, LPR>(ix, w, 1, qsq, lane);
+        uint32_t cur = w.cand_key[0];
+        cmps += 1;
+        __syncwarp();
+        for (int level = ix.levels[u]; level > 0; --level) {
+            bool changed = true;
+            while (changed) {
+                changed = false;
+                const int32_t *list = ix.lists + ix.loff[u] + (int64_t)(level - 1) * ix.hK;
+                int m = 0;
+                for (int c0 = 0; c0 < ix.hK; c0 += 32) {
+                    const int i = c0 + lane;
+                    const int v = i < ix.hK ? __ldg(list + i) : -1;
+                    const unsigned endm = __ballot_sync(kFull, v == -1);
+                    const int nvalid = endm ? __ffs(endm) - 1 : 32;
+                    if (lane < nvalid) w.cand_id[m + lane] = v;
+                    m += nvalid;
+                    if (endm) break;
+                }
+                __syncwarp();
+                if (m == 0) break;
+                compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
+                cmps += m;
+                // first index of the minimum key
+                uint32_t bk = 0xffffffffu;
+                int bj = 0x7fffffff;
+                for (int j = lane; j < m; j += 32) {
+                    uint32_t kj = w.cand_key[j];
+                    if (kj < bk || (kj == bk && j < bj)) { bk = kj; bj = j; }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    uint32_t ok = __shfl_xor_sync(kFull, bk, o);
+                    int oj = __shfl_xor_sync(kFull, bj, o);
+                    if (ok < bk || (ok == bk && oj < bj)) { bk = ok; bj = oj; }
+                }
+                if (bk < cur) {
+                    cur = bk;
+                    u = w.cand_id[bj];
+                    changed = true;
+                }
+                __syncwarp();
+            }
+        }
+        if (lane == 0) {
+            w.cand_id[0] = u;
+            w.cand_key[0] = cur;
+        }
+        __syncwarp();
+        merge(w, S, cap, lb, 1, lane);
+        if (lane == 0) visit(w.tab, w.tbits, u);
+        nvis += 1;
+        __syncwarp();
+    } else {
+        for (int e0 = 0; e0 < ix.nep; e0 += kMaxDegree) {
+            const int m = (ix.nep - e0) < kMaxDegree ? (ix.nep - e0) : kMaxDegree;
+            for (int j = lane; j < m; j += 32) w.cand_id[j] = __ldg(ix.eps + e0 + j);
+            __syncwarp();
+            compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
+            cmps += m;
+            merge(w, S, cap, lb, m, lane);
+            for (int j = lane; j < m; j += 32) visit(w.tab, w.tbits, w.cand_id[j]);
+            nvis += m;
+            __syncwarp();
+            if (nvis > tlimit) { overflow = true; break; }
+        }
+    }
+
+    // ---- SearchImpl2 (graph_searcher.hpp:196-224) ----
+    const int lim = ef_expand < cap ? ef_expand : cap;
+    while (!overflow) {
+        const int f = first_unchecked(w.pid, lb, S < lim ? S : lim, lane);
+        if (f >= S || f >= lim) break;
+        if (nvis + ix.K > tlimit) { overflow = true; break; }
+        const int32_t raw = w.pid[f];
+        __syncwarp();
+        if (lane == 0) w.pid[f] = raw | kChecked;
+        const int u = raw & kIdMask;
+        lb = f + 1;
+        // adjacency row, stop at the first -1; skip repeats within the row and visited ids
+        const int32_t *row = ix.adj + (size_t)u * (size_t)ix.K;
+        int m = 0;
+        for (int c0 = 0; c0 < ix.K; c0 += 32) {
+            const int i = c0 + lane;
+            const int v = i < ix.K ? __ldg(row + i) : -1;
+            const unsigned endm = __ballot_sync(kFull, v == -1);
+            const int nvalid = endm ? __ffs(endm) - 1 : 32;
+            const bool valid = lane < nvalid;
+            const unsigned same = __match_any_sync(kFull, v);
+            const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
+            const bool first = valid && ((same & vmask & lanemask_lt()) == 0);
+            const bool fresh = first && visit(w.tab, w.tbits, v);
+            const unsigned nm = __ballot_sync(kFull, fresh);
+            if (fresh) w.cand_id[m + __popc(nm & lanemask_lt())] = v;
+            m += __popc(nm);
+            if (endm) break;
+        }
+        __syncwarp();
+        nvis += m;
+        if (m == 0) continue;
+        compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
+        cmps += m;
+        merge(w, S, cap, lb, m, lane);
+        if (L.prefetch) {
+            // LinearPool insert success -> graph.prefetch (graph_searcher.hpp:189-191): pull the
+            // adjacency rows of the first few pool entries towards L2
+            const int i = lb + lane;
+            if (lane < 4 && i < S && w.pid[i] >= 0) {
+                const int32_t *r = ix.adj + (size_t)(w.pid[i] & kIdMask) * (size_t)ix.K;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(r));
+            }
+        }
+    }
+
+    // ---- results ----
+    int32_t *oid = bv.out_ids + (size_t)qi * (size_t)bv.out_stride;
+    float *odis = bv.out_dis ? bv.out_dis + (size_t)qi * (size_t)bv.out_stride : nullptr;
+    if (overflow) {
+        for (int j = lane; j < bv.out_stride; j += 32) {
+            oid[j] = -1;
+            if (odis) odis[j] = __int_as_float(0x7f800000);
+        }
+        if (lane == 0) {
+            bv.status[qi] = 1;
+            atomicAdd(bv.overflow, 1u);
+            if (bv.cmps) bv.cmps[qi] = cmps;
+        }
+        __syncwarp();
+        return;
+    }
+    if (!refine) {
+        // to_sorted (neighbor.hpp:421-428); entries past the pool size are reported as -1/inf
+        for (int j = lane; j < bv.out_stride; j += 32) {
+            int32_t id = -1;
+            float dv = __int_as_float(0x7f800000);
+            if (j < kq && j < S) {
+                id = w.pid[j] & kIdMask;
+                dv = IsIntKind<KIND>::value ? dist_of_key_int(w.pkey[j]) : dist_of_key_float(w.pkey[j]);
+            }
+            oid[j] = id;
+            if (odis) odis[j] = dv;
+        }
+    } else {
+        // Refiner::RefineImpl (refiner.hpp:92-110): FP32 distances of the first reorder_k ids,
+        // k smallest by (distance, id), ascending
+        const int avail = S < rk ? S : rk;
+        int32_t *rid = w.pid;
+        float *rdis = reinterpret_cast<float *>(w.pkey);
+        for (int j = lane; j < avail; j += 32) rid[j] &= kIdMask;
+        __syncwarp();
+        // the refiner is FP32Quantizer<metric> with the searcher's metric, even where the first
+        // pass compares codes by L2 (SQ4U)
+        if (ix.metric == M_IP) refine_dists<M_IP>(ix, rid, rdis, avail, w.fq, lane);
+        else refine_dists<M_L2>(ix, rid, rdis, avail, w.fq, lane);
+        for (int j = lane; j < avail; j += 32) {
+            const float dj = rdis[j];
+            const int32_t ij = rid[j];
+            int rank = 0;
+            for (int i = 0; i < avail; ++i) {
+                const float di = rdis[i];
+                rank += (di < dj) || (di == dj && rid[i] < ij);
+            }
+            if (rank < kq) {
+                oid[rank] = ij;
+                if (odis) odis[rank] = dj;
+            }
+        }
+        const int nout = avail < kq ? avail : kq;
+        for (int j = nout + lane; j < bv.out_stride; j += 32) {
+            oid[j] = -1;
+            if (odis) odis[j] = __int_as_float(0x7f800000);
+        }
+    }
+    if (lane == 0) {
+        bv.status[qi] = 0;
+        if (bv.cmps) bv.cmps[qi] = cmps;
+    }
+    __syncwarp();
+}
+
+template <int KIND, int METRIC, int LPR>
+__global__ void __launch_bounds__(256) search_kernel(IndexView ix, BatchView bv, WarpLayout L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    unsigned char *ws = smem + (size_t)wib * (size_t)L.total;
+    WarpState w;
+    w.pkey = reinterpret_cast<uint32_t *>(ws + L.pool_key);
+    w.pid = reinterpret_cast<int32_t *>(ws + L.pool_id);
+    w.cand_id = reinterpret_cast<int32_t *>(ws + L.cand_id);
+    w.cand_key = reinterpret_cast<uint32_t *>(ws + L.cand_key);
+    w.acc_ub = reinterpret_cast<int32_t *>(ws + L.acc_ub);
+    w.acc_key = reinterpret_cast<uint32_t *>(ws + L.acc_key);
+    w.acc_id = reinterpret_cast<int32_t *>(ws + L.acc_id);
+    w.fq = reinterpret_cast<float *>(ws + L.fq);
+    w.qc = reinterpret_cast<uint32_t *>(ws + L.qc);
+    if (L.table_bits > 0) {
+        w.tab = reinterpret_cast<int32_t *>(ws + L.table);
+        w.tbits = L.table_bits;
+    } else {
+        const size_t slot = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
+        w.tab = bv.gtab + (slot << bv.gtab_bits);
+        w.tbits = bv.gtab_bits;
+    }
+    while (true) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(bv.counter, 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= (unsigned)bv.nq) break;
+        const int qi = bv.order ? bv.order[t] : (int)t;
+        search_one<KIND, METRIC, LPR>(ix, bv, L, w, qi, lane);
+    }
+}
+
+// ComputerImpl::operator() for a list of ids (computer.hpp:67-72): one warp per query, the same
+// query encoding and distance engines as the search.  refine=1 uses the FP32 refine store.
+template <int KIND, int METRIC, int LPR>
+__global__ void __launch_bounds__(128) distance_kernel(IndexView ix, int refine, const float *queries, int nq,
+                                                       const int32_t *ids, int m, double *out, WarpLayout L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int qi = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (qi >= nq) return;
+    unsigned char *ws = smem + (size_t)wib * (size_t)L.total;
+    WarpState w;
+    w.pkey = reinterpret_cast<uint32_t *>(ws + L.pool_key);
+    w.pid = reinterpret_cast<int32_t *>(ws + L.pool_id);
+    w.cand_id = reinterpret_cast<int32_t *>(ws + L.cand_id);
+    w.cand_key = reinterpret_cast<uint32_t *>(ws + L.cand_key);
+    w.fq = reinterpret_cast<float *>(ws + L.fq);
+    w.qc = reinterpret_cast<uint32_t *>(ws + L.qc);
+    const float *q = queries + (size_t)qi * (size_t)ix.d;
+    for (int j = lane; j < L.fq_len; j += 32) w.fq[j] = j < ix.d ? q[j] : 0.0f;
+    __syncwarp();
+    const int32_t qsq = prepare_query<KIND, METRIC>(ix, w, lane);
+    for (int c0 = 0; c0 < m; c0 += kMaxDegree) {
+        const int mm = (m - c0) < kMaxDegree ? (m - c0) : kMaxDegree;
+        for (int j = lane; j < mm; j += 32) w.cand_id[j] = ids[(size_t)qi * m + c0 + j];
+        __syncwarp();
+        if (refine) {
+            float *fo = reinterpret_cast<float *>(w.pkey);
+            if (ix.metric == M_IP) refine_dists<M_IP>(ix, w.cand_id, fo, mm, w.fq, lane);
+            else refine_dists<M_L2>(ix, w.cand_id, fo, mm, w.fq, lane);
+            for (int j = lane; j < mm; j += 32) out[(size_t)qi * m + c0 + j] = (double)fo[j];
+        } else {
+            compute_dists<KIND, METRIC, LPR>(ix, w, mm, qsq, lane);
+            for (int j = lane; j < mm; j += 32) {
+                const uint32_t k = w.cand_key[j];
+                out[(size_t)qi * m + c0 + j] =
+                    IsIntKind<KIND>::value ? (double)dist_of_key_int(k) : (double)dist_of_key_float(k);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int KIND, int METRIC, int LPR>
+struct DistF {
+    static cudaError_t run(const IndexView &ix, int refine, const float *queries, int nq, const int32_t *ids, int m,
+                           double *out, cudaStream_t st) {
+        WarpLayout L;
+        make_layout(ix, 2 * kMaxDegree, 0, 0, &L);
+        const int wpb = 4;
+        const size_t smem = (size_t)wpb * L.total;
+        auto k = distance_kernel<KIND, METRIC, LPR>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<(nq + wpb - 1) / wpb, wpb * 32, smem, st>>>(ix, refine, queries, nq, ids, m, out, L);
+        return cudaGetLastError();
+    }
+};
+
+template <int KIND, int METRIC, int LPR>
+cudaError_t launch_t(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st) {
+    const size_t smem = (size_t)cfg.warps_per_block * (size_t)cfg.L.total;
+    auto k = search_kernel<KIND, METRIC, LPR>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<cfg.blocks, cfg.warps_per_block * 32, smem, st>>>(ix, bv, cfg.L);
+    return cudaGetLastError();
+}
+
+template <int KIND, int METRIC, int LPR>
+int occ_t(const LaunchCfg &cfg) {
+    const size_t smem = (size_t)cfg.warps_per_block * (size_t)cfg.L.total;
+    auto k = search_kernel<KIND, METRIC, LPR>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, cfg.warps_per_block * 32, smem) != cudaSuccess) return 0;
+    return nb;
+}
+
+template <template <int, int, int> class F, typename... A>
+auto dispatch(int kind, int metric, int lpr, A &&...a) {
+    const bool ip = metric == M_IP;
+    switch (kind) {
+        case K_SQ4U:  // L2 on codes for both metrics (sq4u_quant.hpp:343)
+            if (lpr >= 4) return F<K_SQ4U, M_L2, 4>::run(a...);
+            if (lpr == 2) return F<K_SQ4U, M_L2, 2>::run(a...);
+            return F<K_SQ4U, M_L2, 1>::run(a...);
+        case K_SQ8U:
+            if (ip) {
+                if (lpr >= 4) return F<K_SQ8U, M_IP, 4>::run(a...);
+                if (lpr == 2) return F<K_SQ8U, M_IP, 2>::run(a...);
+                return F<K_SQ8U, M_IP, 1>::run(a...);
+            }
+            if (lpr >= 4) return F<K_SQ8U, M_L2, 4>::run(a...);
+            if (lpr == 2) return F<K_SQ8U, M_L2, 2>::run(a...);
+            return F<K_SQ8U, M_L2, 1>::run(a...);
+        case K_E5M2:
+            if (ip) return lpr == 1 ? F<K_E5M2, M_IP, 1>::run(a...) : F<K_E5M2, M_IP, 4>::run(a...);
+            return lpr == 1 ? F<K_E5M2, M_L2, 1>::run(a...) : F<K_E5M2, M_L2, 4>::run(a...);
+        default:
+            if (ip) return lpr == 1 ? F<K_FP32, M_IP, 1>::run(a...) : F<K_FP32, M_IP, 4>::run(a...);
+            return lpr == 1 ? F<K_FP32, M_L2, 1>::run(a...) : F<K_FP32, M_L2, 4>::run(a...);
+    }
+}
+
+template <int KIND, int METRIC, int LPR>
+struct LaunchF {
+    static cudaError_t run(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st) {
+        return launch_t<KIND, METRIC, LPR>(ix, bv, cfg, st);
+    }
+};
+template <int KIND, int METRIC, int LPR>
+struct OccF {
+    static int run(const LaunchCfg &cfg) { return occ_t<KIND, METRIC, LPR>(cfg); }
+};
+
+}  // namespace
+
+cudaError_t launch_search(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st) {
+    return dispatch<LaunchF>(ix.kind, ix.metric, cfg.lanes_per_row, ix, bv, cfg, st);
+}
+
+int search_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg) {
+    return dispatch<OccF>(ix.kind, ix.metric, cfg.lanes_per_row, cfg);
+}
+
+cudaError_t launch_distances(const IndexView &ix, int refine, const float *queries, int nq, const int32_t *ids,
+                             int m, double *out, cudaStream_t st) {
+    if (nq <= 0 || m <= 0) return cudaSuccess;
+    return dispatch<DistF>(ix.kind, ix.metric, 1, ix, refine, queries, nq, ids, m, out, st);
+}
+
+bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, WarpLayout *L) {
+    auto up = [](int x, int a) { return (x + a - 1) / a * a; };
+    const int capa = up(cap + 1, 32);
+    int off = 0;
+    L->pool_key = off; off += capa * 4;
+    L->pool_id = off; off += capa * 4;
+    L->cand_id = off; off += kMaxDegree * 4;
+    L->cand_key = off; off += kMaxDegree * 4;
+    L->acc_ub = off; off += kMaxDegree * 4;
+    L->acc_key = off; off += kMaxDegree * 4;
+    L->acc_id = off; off += kMaxDegree * 4;
+    int fq = ix.d;
+    if (ix.kind == K_E5M2 || ix.kind == K_FP32) fq = fq > ix.dalign ? fq : ix.dalign;
+    if (ix.has_refine) fq = fq > ix.r_dalign ? fq : ix.r_dalign;
+    fq = up(fq, 16);
+    L->fq = off; off += fq * 4;
+    L->fq_len = fq;
+    L->qc = off;
+    if (ix.kind == K_SQ4U) off += up(2 * ix.csize, 16);
+    else if (ix.kind == K_SQ8U) off += up(ix.csize, 16);
+    L->table = off;
+    if (table_bits > 0) off += (1 << table_bits) * 4;
+    L->total = up(off, 16);
+    L->cap = capa - 1;
+    L->table_bits = table_bits;
+    L->prefetch = prefetch;
+    return L->total <= 227 * 1024;
+}
+
+}  // namespace gsx

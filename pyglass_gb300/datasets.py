@@ -1,0 +1,80 @@
+"""Seeded synthetic stand-ins for the benchmark workloads of the graph-search path.
+
+The reference measures on ann-benchmarks HDF5 sets (python/ann_dataset/dataset.py:68-88) that are
+not available offline; these generators produce inputs with the shapes and value distributions
+of the named workloads instead.  numpy's PCG64 streams are identical on x86 and aarch64, so the
+same call returns the same bytes on every host; ``checksum`` lets a caller verify that.
+"""
+
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+
+_CHUNK = 100_000
+
+
+def gaussian(n: int, d: int, seed: int, stream: int = 0) -> np.ndarray:
+    """n x d i.i.d. N(0,1) float32 rows."""
+    rng = np.random.default_rng([seed, stream])
+    return rng.standard_normal((n, d), dtype=np.float32)
+
+
+def cluster_mixture(n: int, d: int = 128, n_clusters: int = 1024, sigma: float = 12.0, seed: int = 2,
+                    stream: int = 0) -> np.ndarray:
+    """Gaussian-mixture rows: centers uniform in [0,128]^d (shared by every stream of a seed),
+    per-dimension sigma, rounded and clipped to the integers 0..255, stored float32."""
+    centers = np.random.default_rng([seed, 999]).uniform(0.0, 128.0, size=(n_clusters, d))
+    rng = np.random.default_rng([seed, stream])
+    out = np.empty((n, d), np.float32)
+    for s in range(0, n, _CHUNK):
+        m = min(_CHUNK, n - s)
+        lab = rng.integers(0, n_clusters, size=m)
+        x = centers[lab] + rng.normal(0.0, sigma, size=(m, d))
+        out[s:s + m] = np.clip(np.rint(x), 0, 255)
+    return out
+
+
+def low_rank(n: int, d: int = 960, rank: int = 32, noise: float = 0.05, seed: int = 3, stream: int = 0) -> np.ndarray:
+    """x = W z + e with z ~ N(0, I_rank), W (d x rank) ~ N(0, 1/rank) shared per seed, e ~ N(0, noise^2)."""
+    w = np.random.default_rng([seed, 999]).normal(0.0, 1.0 / np.sqrt(rank), size=(d, rank)).astype(np.float32)
+    rng = np.random.default_rng([seed, stream])
+    out = np.empty((n, d), np.float32)
+    for s in range(0, n, _CHUNK):
+        m = min(_CHUNK, n - s)
+        z = rng.standard_normal((m, rank), dtype=np.float32)
+        e = rng.standard_normal((m, d), dtype=np.float32) * np.float32(noise)
+        out[s:s + m] = z @ w.T + e
+    return out
+
+
+def normalized_mixture(n: int, d: int = 768, n_clusters: int = 4096, sigma: float = 0.3, seed: int = 4,
+                       stream: int = 0) -> np.ndarray:
+    """Unit-length rows of a Gaussian mixture (centers ~ N(0, I), within-cluster sigma)."""
+    centers = np.random.default_rng([seed, 999]).standard_normal((n_clusters, d), dtype=np.float32)
+    rng = np.random.default_rng([seed, stream])
+    out = np.empty((n, d), np.float32)
+    for s in range(0, n, _CHUNK):
+        m = min(_CHUNK, n - s)
+        lab = rng.integers(0, n_clusters, size=m)
+        x = centers[lab] + rng.standard_normal((m, d), dtype=np.float32) * np.float32(sigma)
+        x /= np.linalg.norm(x, axis=1, keepdims=True)
+        out[s:s + m] = x
+    return out
+
+
+# name -> (base generator, query generator, description).  Queries use stream 1 of the same seed.
+WORKLOADS = {
+    "gauss10k": dict(base=lambda: gaussian(10_000, 128, seed=1), queries=lambda: gaussian(1_000, 128, seed=1, stream=1),
+                     index=("HNSW", 32, 50, "FP32"), metric="L2",
+                     desc="10,000 x 128 N(0,1), HNSW R=32 L=50, 1,000 queries"),
+    "clusters1m": dict(base=lambda: cluster_mixture(1_000_000), queries=lambda: cluster_mixture(10_000, stream=1),
+                       index=("NSG", 32, 50, "SQ8U"), metric="L2",
+                       desc="1,000,000 x 128 from 1,024 clusters (sigma 12, integers 0..255), NSG R=32 L=50 "
+                            "(build quant SQ8U), 10,000 queries"),
+}
+
+
+def checksum(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()[:16]

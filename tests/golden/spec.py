@@ -1,0 +1,36 @@
+"""What the golden fixtures contain; shared by the generator and the tests."""
+
+import itertools
+
+from pyglass_gb300 import datasets
+
+N, D = 3000, 100          # d=100 exercises the padding of every quantizer (dalign 112 / 128)
+NQ_DIST, NQ_SEARCH = 16, 60
+GRAPHS = {"hnsw_d100": ("HNSW", 16, 40), "nsg_d100": ("NSG", 16, 40)}
+QUANTS = [("SQ8U", "L2"), ("SQ8U", "IP"), ("SQ4U", "L2"), ("SQ4U", "IP"), ("E5M2", "L2"), ("E5M2", "IP"),
+          ("FP32", "L2"), ("FP32", "IP")]
+# (quant, metric, refine)
+SEARCHERS = [("SQ8U", "L2", ""), ("SQ8U", "IP", ""), ("SQ4U", "L2", "FP32"), ("SQ4U", "IP", "FP32"),
+             ("E5M2", "L2", ""), ("E5M2", "IP", ""), ("FP32", "L2", ""), ("FP32", "IP", ""), ("SQ8U", "L2", "FP32")]
+# (ef, k): includes k > ef, the case where search and batch_search differ (graph_searcher.hpp:134,152)
+EFK = [(16, 10), (40, 10), (8, 20)]
+
+
+def base():
+    return datasets.gaussian(N, D, seed=11)
+
+
+def queries():
+    return datasets.gaussian(NQ_SEARCH, D, seed=11, stream=1)
+
+
+def search_cases():
+    for g, (q, m, r), (ef, k), mode in itertools.product(GRAPHS, SEARCHERS, EFK, ["batch", "single"]):
+        if mode == "single" and ef != 8:
+            continue
+        yield (g, q, m, r, ef, k, mode)
+
+
+def case_key(c):
+    g, q, m, r, ef, k, mode = c
+    return f"{g}/{q}/{m}/{r or '-'}/{ef}/{k}/{mode}"

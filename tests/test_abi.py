@@ -1,0 +1,150 @@
+"""CPU checks of the C ABI: the library loads, exports every declared entry point, and its
+host-side logic (graph files, argument checks, error codes) works without a GPU."""
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.helpers import write_glass
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "glass_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib(glass):
+    return C.CDLL(os.path.join(ROOT, "pyglass_gb300", "libglass_gb300.so"))
+
+
+def declared():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(gsx_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def _load(lib, path, fmt="glass"):
+    lib.gsx_graph_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]
+    h = C.c_void_p()
+    rc = lib.gsx_graph_load(path.encode(), fmt.encode(), C.byref(h))
+    return rc, h
+
+
+def _info(lib, h):
+    lib.gsx_graph_info.argtypes = [C.c_void_p] + [C.POINTER(C.c_int32)] * 4
+    v = [C.c_int32() for _ in range(4)]
+    assert lib.gsx_graph_info(h, *[C.byref(x) for x in v]) == 0
+    return [x.value for x in v]
+
+
+def _adj(lib, h, N, K):
+    out = np.zeros((N, K), np.int32)
+    lib.gsx_graph_adjacency.argtypes = [C.c_void_p, C.c_void_p]
+    assert lib.gsx_graph_adjacency(h, out.ctypes.data) == 0
+    return out
+
+
+def test_glass_roundtrip_with_hnsw_levels(lib, tmp_path):
+    rng = np.random.default_rng(0)
+    N, K = 50, 8
+    adj = rng.integers(-1, N, size=(N, K)).astype(np.int32)
+    lists = [np.zeros(0, np.int32) for _ in range(N)]
+    lists[3] = np.array([7, 9, -1, -1], np.int32)  # node 3 on level 1, hK = 4
+    lists[7] = np.array([3, -1, -1, -1], np.int32)
+    lists[9] = np.array([3, 7, -1, -1], np.int32)
+    p = str(tmp_path / "a.glass")
+    write_glass(p, adj, [3], hnsw=(4, 3, lists))
+    rc, h = _load(lib, p)
+    assert rc == 0
+    assert _info(lib, h) == [N, K, 1, 1]
+    np.testing.assert_array_equal(_adj(lib, h, N, K), adj)
+    q = str(tmp_path / "b.glass")
+    lib.gsx_graph_save.argtypes = [C.c_void_p, C.c_char_p]
+    assert lib.gsx_graph_save(h, q.encode()) == 0
+    assert open(p, "rb").read() == open(q, "rb").read()
+    lib.gsx_graph_destroy.argtypes = [C.c_void_p]
+    lib.gsx_graph_destroy(h)
+
+
+def test_reference_graph_fixture_loads(lib):
+    rc, h = _load(lib, os.path.join(ROOT, "tests", "golden", "hnsw_d100.glass"))
+    assert rc == 0
+    N, K, nep, hn = _info(lib, h)
+    assert (N, K, hn) == (3000, 16, 1)
+
+
+def test_nsg_and_diskann_formats(lib, tmp_path):
+    rows = [[1, 2], [0], [0, 1, 3], []]
+    K, ep = 3, 2
+    p = str(tmp_path / "g.nsg")
+    with open(p, "wb") as f:  # graph.hpp:354-379
+        np.array([K, ep], np.int32).tofile(f)
+        for r in rows:
+            np.array([len(r)] + r, np.int32).tofile(f)
+    rc, h = _load(lib, p, "nsg")
+    assert rc == 0
+    assert _info(lib, h)[:3] == [4, 3, 1]
+    want = np.full((4, 3), -1, np.int32)
+    for i, r in enumerate(rows):
+        want[i, : len(r)] = r
+    np.testing.assert_array_equal(_adj(lib, h, 4, 3), want)
+    p2 = str(tmp_path / "g.diskann")
+    body = b"".join(np.array([len(r)] + r, np.int32).tobytes() for r in rows)
+    with open(p2, "wb") as f:  # graph.hpp:289-316
+        np.array([24 + len(body)], np.uint64).tofile(f)
+        np.array([K, ep], np.int32).tofile(f)
+        np.array([0], np.uint64).tofile(f)
+        f.write(body)
+    rc, h2 = _load(lib, p2, "diskann")
+    assert rc == 0
+    np.testing.assert_array_equal(_adj(lib, h2, 4, 3), want)
+
+
+def test_malformed_graphs_are_rejected(lib, tmp_path):
+    p = str(tmp_path / "bad.glass")
+    write_glass(p, np.array([[1, 5], [0, -1]], np.int32), [0])  # id 5 >= N
+    rc, _ = _load(lib, p)
+    assert rc == 1
+    lib.gsx_last_error.restype = C.c_char_p
+    assert b"out of range" in lib.gsx_last_error()
+    rc, _ = _load(lib, str(tmp_path / "missing.glass"))
+    assert rc == 5
+    rc, _ = _load(lib, p, "unknown-format")
+    assert rc == 1
+    # an HNSW neighbour that does not exist on the level it is listed on
+    p3 = str(tmp_path / "bad_hnsw.glass")
+    lists = [np.zeros(0, np.int32), np.array([0, -1], np.int32)]
+    write_glass(p3, np.array([[1], [0]], np.int32), [1], hnsw=(2, 1, lists))
+    rc, _ = _load(lib, p3)
+    assert rc == 1
+
+
+def test_degree_limit(lib, tmp_path):
+    p = str(tmp_path / "wide.glass")
+    write_glass(p, np.zeros((2, 65), np.int32), [0])
+    rc, _ = _load(lib, p)
+    assert rc == 7  # GSX_ERR_UNSUPPORTED
+
+
+def test_python_surface(glass):
+    for name in ["Graph", "Searcher", "set_num_threads"]:
+        assert hasattr(glass, name)
+    g = glass.Graph(os.path.join(ROOT, "tests", "golden", "nsg_d100.glass"))
+    assert g.info()[:2] == (3000, 16)
+    glass.set_num_threads(4)
+
+
+def test_no_device_is_an_error_not_a_fallback(glass):
+    if glass.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    g = glass.Graph(os.path.join(ROOT, "tests", "golden", "nsg_d100.glass"))
+    with pytest.raises(RuntimeError, match="no CUDA device"):
+        glass.Searcher(g, np.zeros((3000, 100), np.float32), "L2", "SQ8U")

@@ -1,0 +1,43 @@
+"""Full-size parity on the 1M x 128 clustered workload (NSG R=32 built by the reference): the GPU
+batch equals the oracle on a query sample, and size-independent properties hold for all queries."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from pyglass_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GRAPH = os.path.join(ROOT, "data", "clusters1m.glass")
+
+
+@pytest.fixture(scope="module")
+def workload():
+    if not os.path.exists(GRAPH):
+        pytest.skip("data/clusters1m.glass not present (built by oracle/build_graphs.py)")
+    meta = json.load(open(GRAPH.replace(".glass", ".json")))
+    w = datasets.WORKLOADS["clusters1m"]
+    base, q = w["base"](), w["queries"]()
+    assert datasets.checksum(base) == meta["base_checksum"], "synthetic base differs from the one the graph was built on"
+    return base, q
+
+
+def test_clusters1m_sq4u_refine_matches_oracle(gpu, oracle, workload):
+    base, q = workload
+    s = gpu.Searcher(gpu.Graph(GRAPH), base, "L2", "SQ4U", "FP32")
+    o = oracle.Searcher(oracle.Graph(GRAPH), base, "L2", "SQ4U", "FP32")
+    for ef in (16, 64):
+        s.set_ef(ef)
+        o.set_ef(ef)
+        gi, gd = s.batch_search(q, 10)
+        sample = np.arange(0, q.shape[0], 25)
+        oi, od = o.batch_search(q[sample], 10)
+        np.testing.assert_array_equal(gi[sample], oi)
+        np.testing.assert_array_equal(gd[sample], od)
+        # properties over all queries: sorted distances, unique valid ids
+        assert np.all(np.diff(gd, axis=1) >= 0)
+        assert np.all((gi >= 0) & (gi < base.shape[0]))
+        assert all(len(set(r)) == r.size for r in gi)
