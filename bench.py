@@ -1,0 +1,338 @@
+"""Benchmark of the GB300 graph-search path on the 1M x 128 clustered workload.
+
+Workload (synthetic stand-in, seeded; the reference's ann-benchmarks sets are not available):
+1,000,000 x 128 base vectors from 1,024 Gaussian clusters (integers 0..255), 10,000 queries from
+the same mixture, NSG graph R=32 L=50 built by the reference's CPU builder (data/clusters1m.glass,
+made by oracle/build_graphs.py), searcher SQ4U + FP32 refine, k=10.
+
+A step is one batched search of all 10,000 queries at the headline ef.  `value` is QPS with the
+queries resident in HBM (CUDA events on the launching stream, L2 flushed by a 512 MB write
+between steps); `e2e` is the same batch through the public API (Searcher.batch_search) with
+host numpy buffers, copies included.  One JSON line is printed by rank 0.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--ef 128] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "QPS at recall@10>=0.95 (1M×128, SQ4U), batched/served vs plain; p50/p99 latency"
+WORKLOAD = "clusters1m"
+GRAPH = os.path.join(ROOT, "data", f"{WORKLOAD}.glass")
+SWEEP_EF = [16, 32, 64, 128]
+K = 10
+
+
+def args_():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--ef", type=int, default=128)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--cpu-sample", type=int, default=2000, help="queries per CPU-baseline step")
+    p.add_argument("--profile", action="store_true",
+                   help="only the warm-up and timed device launches (default tuning), for ncu captures")
+    return p.parse_args()
+
+
+def load_workload():
+    from pyglass_gb300 import datasets
+
+    if not os.path.exists(GRAPH):
+        raise SystemExit(json.dumps({"error": f"{GRAPH} missing: run python oracle/build_graphs.py {WORKLOAD}"}))
+    meta = json.load(open(GRAPH.replace(".glass", ".json")))
+    w = datasets.WORKLOADS[WORKLOAD]
+    base, queries = w["base"](), w["queries"]()
+    if datasets.checksum(base) != meta["base_checksum"]:
+        raise SystemExit(json.dumps({"error": "synthetic base differs from the one the graph was built on"}))
+    return base, queries, meta
+
+
+def workload_config(ef, nq, extra=None):
+    c = {"workload": "1,000,000 x 128 from 1,024 clusters (sigma 12, integers 0..255); NSG R=32 L=50 built by "
+                     "the reference CPU builder; 10,000 queries; SQ4U + FP32 refine (reorder 15); k=10",
+         "nq": nq, "k": K, "ef": ef, "metric": "L2", "quantizer": "SQ4U", "refine_quant": "FP32"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def cpu_baseline(base, queries, ef, sample):
+    """The oracle (C restatement of the reference searcher, OpenMP over all host cores) on a
+    bounded sample of the workload."""
+    from oracle import pyoracle
+
+    pyoracle.build(ref=False)
+    g = pyoracle.Graph(GRAPH)
+    s = pyoracle.Searcher(g, base, "L2", "SQ4U", "FP32")
+    s.set_ef(ef)
+    q = queries[:sample]
+    s.batch_search(q[:200], K)  # warm-up
+    best = 1e30
+    for _ in range(3):
+        t = time.perf_counter()
+        s.batch_search(q, K)
+        best = min(best, time.perf_counter() - t)
+    cores = os.cpu_count() or 1
+    return {"value": sample / best, "unit": "QPS", "cores": cores, "kind": "port",
+            "sample": f"{sample} of the 10,000 queries at ef={ef}, best of 3, {cores} OpenMP threads"}, s
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.p is None:
+            return
+        time.sleep(0.3)
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                self.rows.append(f)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def ground_truth(torch, base_t, q_t, k):
+    """Exact k nearest neighbours (fp32; the data are integers, so the products are exact)."""
+    xn = (base_t * base_t).sum(1)
+    out = []
+    for s in range(0, q_t.shape[0], 500):
+        d = xn[None, :] - 2.0 * (q_t[s:s + 500] @ base_t.T)
+        out.append(torch.topk(d, k, dim=1, largest=False).indices.int())
+    return torch.cat(out).cpu().numpy()
+
+
+def recall(ids, gt):
+    return float(np.mean([len(np.intersect1d(ids[i, :K], gt[i, :K])) for i in range(ids.shape[0])])) / K
+
+
+def measured_peak():
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(mp["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    base, queries, meta = load_workload()
+    sample = min(a.cpu_sample, queries.shape[0])
+    cb, s = cpu_baseline(base, queries, a.ef, sample)
+    q = queries[:sample]
+    for _ in range(a.warmup):
+        s.batch_search(q, K)
+    times = []
+    for _ in range(a.steps):
+        t = time.perf_counter()
+        s.batch_search(q, K)
+        times.append(time.perf_counter() - t)
+    ms = 1000 * statistics.mean(times)
+    value = sample / (ms / 1000)
+    cb["value"] = value
+    cb["sample"] = f"{sample} of the 10,000 queries per step at ef={a.ef}, {cb['cores']} OpenMP threads"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "QPS", "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u4+f32", "data": "synthetic", "config": workload_config(a.ef, sample),
+        "cpu_baseline": cb, "e2e": {"value": value, "unit": "QPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference searcher restated in C (oracle/glass_oracle.c, bit-exact with the compiled reference "
+                "on x86); the reference sources are not present on the GPU host, so it cannot be compiled there"}))
+
+
+def run_gpu(a):
+    import torch
+
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from pyglass_gb300 import glass
+
+    base, queries, meta = load_workload()
+    nq, d = queries.shape
+    s = glass.Searcher(glass.Graph(GRAPH), base, "L2", "SQ4U", "FP32", device=local)
+    s.set_ef(a.ef)
+    if not a.profile:
+        s.optimize()
+    tuning = s.get_tuning()
+    stream = torch.cuda.current_stream()
+    dq = torch.from_numpy(queries).cuda()
+    ids = torch.empty((nq, K), dtype=torch.int32, device="cuda")
+    dis = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+    cmps = torch.empty(nq, dtype=torch.int32, device="cuda")
+    exps = torch.empty(nq, dtype=torch.int32, device="cuda")
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 512 MB > L2
+
+    def launch():
+        s.batch_search_device(dq.data_ptr(), nq, K, ids.data_ptr(), dis.data_ptr(), cmps=cmps.data_ptr(),
+                              expansions=exps.data_ptr(), kmax=K, stream=stream.cuda_stream)
+
+    for _ in range(a.warmup):
+        flush.zero_()
+        launch()
+    torch.cuda.synchronize()
+    assert s.overflow_count() == 0
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    if a.profile:
+        print(json.dumps({"profile": True, "ef": a.ef, "step_ms": step_ms, "tuning": tuning}))
+        return
+    total_s = sum(step_ms) / 1000.0
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * nq * a.steps / total_s
+    ms_per_step = 1000.0 * total_s / a.steps
+
+    # algorithmic bytes of one launch: per query n_dist*csize + n_expand*4K + reorder_k rows of
+    # the fp32 refine store + the query row + the k (id, dist) results
+    c = cmps.cpu().numpy().astype(np.int64)
+    x = exps.cpu().numpy().astype(np.int64)
+    csize, Kdeg, reorder = 64, 32, 15
+    alg_bytes = int((c * csize).sum() + (x * 4 * Kdeg).sum() + nq * (reorder * 4 * 128 + 4 * d + 8 * K))
+    kern_s = statistics.mean(step_ms) / 1000.0
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / kern_s / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get(f"search_sq4u_{WORKLOAD}_ef{a.ef}")
+
+    out_ids = ids.cpu().numpy()
+    base_t = torch.from_numpy(base).cuda()
+    gt = ground_truth(torch, base_t, dq, K)
+    del base_t
+    rec = recall(out_ids, gt)
+
+    # ef sweep (one timed batch each)
+    sweep = []
+    for ef in SWEEP_EF:
+        s.set_ef(ef)
+        launch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.zero_()
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sweep.append({"ef": ef, "qps": nq / (e0.elapsed_time(e1) / 1000), "recall@10": recall(ids.cpu().numpy(), gt),
+                      "avg_dist_cmps": float(cmps.float().mean().item())})
+    s.set_ef(a.ef)
+
+    # e2e: the public API with host buffers (copies in the timed region)
+    for _ in range(2):
+        s.batch_search(queries, K)
+    e2e_t = []
+    for _ in range(max(3, a.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.batch_search(queries, K)
+        e2e_t.append(time.perf_counter() - t)
+    e2e = {"value": nq / statistics.mean(e2e_t), "unit": "QPS", "h2d_bytes_per_step": nq * d * 4,
+           "d2h_bytes_per_step": nq * K * 8 + nq * 4 + 4}
+
+    # plain per-query GPU form: one search call per query
+    lat = []
+    for i in range(200):
+        t = time.perf_counter()
+        s.search(queries[i], K)
+        lat.append(time.perf_counter() - t)
+    lat_ms = np.array(lat[20:]) * 1000
+    plain = {"qps": 1000.0 / float(lat_ms.mean()), "p50_ms": float(np.percentile(lat_ms, 50)),
+             "p99_ms": float(np.percentile(lat_ms, 99)), "queries": int(lat_ms.size)}
+
+    if rank == 0:
+        cb, _ = cpu_baseline(base, queries, a.ef, min(a.cpu_sample, nq))
+        line = {
+            "metric": METRIC, "value": value, "unit": "QPS", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u4+f32", "data": "synthetic",
+            "config": workload_config(a.ef, nq, {"l2": "512 MB buffer written between timed steps (L2 flush)",
+                                                 "tuning": tuning, "parallelism": f"replicas x{world}"}),
+            "recall@10": rec,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": alg_bytes, "avg_dist_cmps": float(c.mean()),
+                         "avg_expansions": float(x.mean())},
+            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": a.steps, "clocks": clk.summary(),
+            "plain_per_query": plain, "batched_over_plain": value / world / plain["qps"], "sweep": sweep,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    a = args_()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -50,6 +50,11 @@ int gsx_device_count(void);
 int gsx_graph_load(const char *filename, const char *format, gsx_graph **out);
 /* Builds a graph from memory: adj is N*K int32 (-1 padded), eps the entry points. */
 int gsx_graph_create(const int32_t *adj, int32_t N, int32_t K, const int32_t *eps, int32_t nep, gsx_graph **out);
+/* Attaches HNSW upper levels (HNSWInitializer, glass/hnsw/HNSWInitializer.hpp:22-86) to a graph:
+ * hK = upper-level degree, ep = entry point, levels[N] = number of upper levels of each node,
+ * lists = the nodes' level lists concatenated in node order (levels[u]*hK int32 each, -1 padded).
+ * The graph is re-validated. */
+int gsx_graph_set_levels(gsx_graph *g, int32_t hK, int32_t ep, const int32_t *levels, const int32_t *lists);
 /* Graph::save (graph.hpp:240-253) in the glass format. */
 int gsx_graph_save(const gsx_graph *g, const char *filename);
 /* N, K, number of entry points, and whether HNSW upper levels are present. */
@@ -89,11 +94,19 @@ int gsx_searcher_search_batch(gsx_searcher *s, const float *queries, int32_t nq,
 
 /* Batched search with per-query ef and k (either array may be NULL = uniform), buffers in
  * DEVICE memory, enqueued on `stream` (cudaStream_t, NULL = the searcher's stream) without a
- * host synchronisation.  Output rows have stride kmax = max k.  cmps (may be NULL) receives
- * per-query distance counts.  No reference counterpart: the batched/persistent form. */
+ * host synchronisation.  Per-query ef values must not exceed the searcher's ef (set_ef) and
+ * per-query k values must not exceed kmax; output rows have stride kmax.  d_cmps / d_expansions
+ * (may be NULL) receive per-query distance and expansion counts.  A query whose shared-memory
+ * visited table would overflow is left as -1/inf and counted (gsx_searcher_overflow_count); the
+ * host-buffer entry points re-run such queries exactly.  No reference counterpart: the
+ * batched/persistent form. */
 int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
                                      const int32_t *d_ef, const int32_t *d_k, int32_t kmax, int32_t *d_ids,
-                                     float *d_dis, int32_t *d_cmps, void *stream);
+                                     float *d_dis, int32_t *d_cmps, int32_t *d_expansions, void *stream);
+
+/* Queries of the last device batch left unanswered because their visited table overflowed
+ * (synchronises the searcher's stream). */
+int gsx_searcher_overflow_count(gsx_searcher *s, uint32_t *count);
 
 /* Same as above with HOST buffers (copies inside), synchronous. */
 int gsx_searcher_search_batch_mixed(gsx_searcher *s, const float *queries, int32_t nq, int32_t k,
@@ -131,6 +144,29 @@ int gsx_searcher_distances(gsx_searcher *s, const float *queries, int32_t nq, co
 
 /* Copies out the encoded base rows (n*code_size bytes) and calibrator parameters (2 floats). */
 int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int32_t *code_size);
+
+/* ---- serving: continuous batching over a resident index (no reference counterpart) -------- */
+
+typedef struct gsx_server gsx_server;
+
+/* Starts a request loop on searcher s: a dispatcher thread admits queued requests (oldest first)
+ * into an arena of max_queries_in_flight device query slots, capped so that the arena takes at
+ * most half of the free device memory, and launches each admitted group on one of `streams` CUDA
+ * streams, so that groups overlap on the device.  kmax / efmax bound the per-request k and ef.
+ * While a server runs, the searcher must not be used directly. */
+int gsx_server_create(gsx_searcher *s, int32_t max_queries_in_flight, int32_t kmax, int32_t efmax, int32_t streams,
+                      gsx_server **out);
+/* Number of query slots actually admitted by free device memory. */
+int gsx_server_capacity(const gsx_server *sv, int32_t *slots);
+/* Queues nq queries (host memory, copied) with their k and ef; returns a ticket at once. */
+int gsx_server_submit(gsx_server *sv, const float *queries, int32_t nq, int32_t k, int32_t ef, uint64_t *ticket);
+/* Waits at most timeout_ms for a ticket; on success writes ids/dis (nq*k each, may be NULL) and the
+ * submit-to-completion latency, and forgets the ticket.  GSX_ERR_TIMEOUT leaves it pending. */
+int gsx_server_wait(gsx_server *sv, uint64_t ticket, int32_t timeout_ms, int32_t *ids, float *dis, double *latency_ms);
+/* Completed queries, queued requests, groups on the device. */
+int gsx_server_stats(gsx_server *sv, int64_t *completed_queries, int32_t *queued_requests, int32_t *running_groups);
+/* Finishes every queued request, then stops the loop and frees its memory. */
+void gsx_server_destroy(gsx_server *sv);
 
 #ifdef __cplusplus
 }

@@ -174,7 +174,7 @@ int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int tabl
 // Enqueues one batch on `st`; nothing is synchronised.
 int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int32_t *d_ef, const int32_t *d_k,
             int kmax, int efmax, int32_t *d_ids, float *d_dis, int32_t *d_cmps, bool single, cudaStream_t st,
-            const LaunchCfg *cfg_in = nullptr) {
+            const LaunchCfg *cfg_in = nullptr, int32_t *d_exp = nullptr) {
     if (nq <= 0) return GSX_OK;
     LaunchCfg cfg;
     if (cfg_in) cfg = *cfg_in;
@@ -199,6 +199,7 @@ int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int3
     bv.out_ids = d_ids;
     bv.out_dis = d_dis;
     bv.cmps = d_cmps;
+    bv.expansions = d_exp;
     bv.status = s->status.as<int32_t>();
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
@@ -316,6 +317,19 @@ int host_batch(gsx_searcher *s, const float *queries, int nq, int k, const int32
 
 }  // namespace
 
+// Hooks of the serving loop (gsx_server.cpp).
+int server_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg) {
+    return make_cfg(s, kmax, efmax, nq, false, 0, cfg);
+}
+
+int server_resolve_one(gsx_searcher *s, const float *q, int k, int ef, int32_t *ids, float *dis) {
+    const int32_t efp = ef;
+    const double keep = s->last_avg_cmps;
+    const int rc = host_batch(s, q, 1, k, &efp, nullptr, k, ids, dis, false);
+    s->last_avg_cmps = keep;
+    return rc;
+}
+
 }  // namespace gsx
 
 using namespace gsx;
@@ -361,6 +375,33 @@ int gsx_graph_create(const int32_t *adj, int32_t N, int32_t K, const int32_t *ep
     }
     *out = g;
     return GSX_OK;
+}
+
+int gsx_graph_set_levels(gsx_graph *g, int32_t hK, int32_t ep, const int32_t *levels, const int32_t *lists) {
+    if (!g || !levels || (hK <= 0)) return fail(GSX_ERR_INVALID, "bad level arguments");
+    HostGraph &h = g->g;
+    if (h.N == 0) return fail(GSX_ERR_STATE, "graph is empty");
+    HostGraph saved = h;
+    h.has_hnsw = 1;
+    h.hK = hK;
+    h.hep = ep;
+    h.levels.assign(levels, levels + h.N);
+    h.loff.assign((size_t)h.N + 1, 0);
+    for (int32_t u = 0; u < h.N; ++u) {
+        if (h.levels[u] < 0) {
+            h = saved;
+            return fail(GSX_ERR_INVALID, "negative level for node %d", u);
+        }
+        h.loff[u + 1] = h.loff[u] + (int64_t)h.levels[u] * hK;
+    }
+    if (h.loff[h.N] > 0 && !lists) {
+        h = saved;
+        return fail(GSX_ERR_INVALID, "null level lists");
+    }
+    h.lists.assign(lists, lists + h.loff[h.N]);
+    int rc = validate_graph(h);
+    if (rc) h = saved;
+    return rc;
 }
 
 int gsx_graph_save(const gsx_graph *g, const char *filename) {
@@ -543,7 +584,7 @@ int gsx_searcher_search_batch_mixed(gsx_searcher *s, const float *queries, int32
 
 int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
                                      const int32_t *d_ef, const int32_t *d_k, int32_t kmax, int32_t *d_ids,
-                                     float *d_dis, int32_t *d_cmps, void *stream) {
+                                     float *d_dis, int32_t *d_cmps, int32_t *d_expansions, void *stream) {
     if (!s || (nq > 0 && (!d_queries || !d_ids))) return fail(GSX_ERR_INVALID, "null argument");
     if (!s->has_data) return fail(GSX_ERR_STATE, "search before set_data");
     if (k <= 0) return fail(GSX_ERR_INVALID, "k must be positive");
@@ -552,7 +593,8 @@ int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, in
     if (rc) return rc;
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
     // with per-query ef on the device the caller's searcher ef is the upper bound
-    return enqueue(s, d_queries, nq, k, s->ef, d_ef, d_k, kmax, s->ef, d_ids, d_dis, d_cmps, false, st);
+    return enqueue(s, d_queries, nq, k, s->ef, d_ef, d_k, kmax, s->ef, d_ids, d_dis, d_cmps, false, st, nullptr,
+                   d_expansions);
 }
 
 int gsx_searcher_get_last_search_avg_dist_cmps(const gsx_searcher *s, double *out) {
@@ -675,6 +717,17 @@ int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int
         if (rc) return rc;
         GSX_CUDA(cudaMemcpy(codes, s->codes.p, (size_t)s->ix.N * s->ix.csize, cudaMemcpyDeviceToHost));
     }
+    return GSX_OK;
+}
+
+int gsx_searcher_overflow_count(gsx_searcher *s, uint32_t *count) {
+    if (!s || !count) return fail(GSX_ERR_INVALID, "null argument");
+    *count = 0;
+    if (!s->counters.p) return GSX_OK;
+    int rc = set_device(s);
+    if (rc) return rc;
+    GSX_CUDA(cudaMemcpyAsync(count, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, s->stream));
+    GSX_CUDA(cudaStreamSynchronize(s->stream));
     return GSX_OK;
 }
 

@@ -47,6 +47,7 @@ struct BatchView {
     int32_t *out_ids;
     float *out_dis;
     int32_t *cmps;            // optional per-query distance counts
+    int32_t *expansions;      // optional per-query expansion counts (adjacency rows read)
     int32_t *status;          // per-query: 0 ok, 1 visited table full (query left unanswered)
     unsigned int *counter;    // work-queue head, zeroed before the launch
     unsigned int *overflow;   // number of overflowed queries

@@ -165,15 +165,21 @@ struct Searcher {
     // Device-resident batch: pointers are integers (e.g. torch tensor data_ptr()); enqueued on
     // `stream` (0 = the searcher's own stream) without synchronising.
     void batch_search_device(uintptr_t queries, int nq, int k, uintptr_t ids, uintptr_t dis, uintptr_t ef_per,
-                             uintptr_t k_per, int kmax, uintptr_t cmps, uintptr_t stream) {
+                             uintptr_t k_per, int kmax, uintptr_t cmps, uintptr_t expansions, uintptr_t stream) {
         int rc;
         {
             py::gil_scoped_release l;
             rc = gsx_searcher_search_batch_device(s, (const float *)queries, nq, k, (const int32_t *)ef_per,
                                                   (const int32_t *)k_per, kmax, (int32_t *)ids, (float *)dis,
-                                                  (int32_t *)cmps, (void *)stream);
+                                                  (int32_t *)cmps, (int32_t *)expansions, (void *)stream);
         }
         check(rc);
+    }
+
+    unsigned overflow_count() {
+        uint32_t c = 0;
+        check(gsx_searcher_overflow_count(s, &c));
+        return c;
     }
 
     py::array_t<double> distances(py::object query, py::object ids, bool refine) {
@@ -252,6 +258,67 @@ struct Searcher {
     }
 };
 
+// The serving loop (gsx_server_*): submit returns a ticket, wait returns (ids, dis, latency_ms).
+struct Server {
+    gsx_server *sv = nullptr;
+    int32_t dim = 0;
+    py::object keep;  // the Searcher must outlive the server
+
+    Server(py::object searcher, int capacity, int kmax, int efmax, int streams) {
+        Searcher &s = searcher.cast<Searcher &>();
+        keep = searcher;
+        dim = s.dim;
+        check(gsx_server_create(s.s, capacity, kmax, efmax, streams, &sv));
+    }
+    ~Server() { close(); }
+    void close() {
+        if (sv) {
+            py::gil_scoped_release l;
+            gsx_server_destroy(sv);
+            sv = nullptr;
+        }
+    }
+    uint64_t submit(py::object query, int k, int ef) {
+        if (!sv) throw std::runtime_error("glass-gb300: server closed");
+        f32arr items(query);
+        size_t nq, features;
+        shape_of(items.request(), &nq, &features);
+        if ((int32_t)features != dim) throw std::runtime_error("glass-gb300: query dimension mismatch");
+        uint64_t t = 0;
+        int rc;
+        {
+            py::gil_scoped_release l;
+            rc = gsx_server_submit(sv, items.data(), (int32_t)nq, k, ef, &t);
+        }
+        check(rc);
+        return t;
+    }
+    py::tuple wait(uint64_t ticket, int nq, int k, int timeout_ms) {
+        if (!sv) throw std::runtime_error("glass-gb300: server closed");
+        py::array_t<int32_t> ids({(py::ssize_t)nq, (py::ssize_t)k});
+        py::array_t<float> dis({(py::ssize_t)nq, (py::ssize_t)k});
+        double lat = 0;
+        int rc;
+        {
+            py::gil_scoped_release l;
+            rc = gsx_server_wait(sv, ticket, timeout_ms, ids.mutable_data(), dis.mutable_data(), &lat);
+        }
+        check(rc);
+        return py::make_tuple(ids, dis, lat);
+    }
+    int capacity() const {
+        int32_t c = 0;
+        check(gsx_server_capacity(sv, &c));
+        return c;
+    }
+    py::tuple stats() {
+        int64_t done = 0;
+        int32_t q = 0, r = 0;
+        check(gsx_server_stats(sv, &done, &q, &r));
+        return py::make_tuple(done, q, r);
+    }
+};
+
 }  // namespace
 
 PYBIND11_MODULE(_glass, m) {
@@ -281,7 +348,8 @@ PYBIND11_MODULE(_glass, m) {
         .def("batch_search_mixed", &Searcher::batch_search_mixed, py::arg("query"), py::arg("ef"), py::arg("k"))
         .def("batch_search_device", &Searcher::batch_search_device, py::arg("queries"), py::arg("nq"), py::arg("k"),
              py::arg("ids"), py::arg("dis"), py::arg("ef_per") = 0, py::arg("k_per") = 0, py::arg("kmax") = 0,
-             py::arg("cmps") = 0, py::arg("stream") = 0)
+             py::arg("cmps") = 0, py::arg("expansions") = 0, py::arg("stream") = 0)
+        .def("overflow_count", &Searcher::overflow_count)
         .def("optimize", &Searcher::optimize, py::arg("num_threads") = 0)
         .def("get_last_search_dist_cmps", &Searcher::get_last_search_avg_dist_cmps)
         .def("distances", &Searcher::distances, py::arg("query"), py::arg("ids"), py::arg("refine") = false)
@@ -291,4 +359,13 @@ PYBIND11_MODULE(_glass, m) {
         .def("set_tuning", &Searcher::set_tuning, py::arg("warps_per_block") = 0, py::arg("table_bits") = 0,
              py::arg("lanes_per_row") = 0, py::arg("prefetch") = 1)
         .def("memory", &Searcher::memory);
+
+    py::class_<Server>(m, "Server")
+        .def(py::init<py::object, int, int, int, int>(), py::arg("searcher"), py::arg("capacity") = 16384,
+             py::arg("kmax") = 100, py::arg("efmax") = 256, py::arg("streams") = 4)
+        .def("submit", &Server::submit, py::arg("query"), py::arg("k"), py::arg("ef"))
+        .def("wait", &Server::wait, py::arg("ticket"), py::arg("nq"), py::arg("k"), py::arg("timeout_ms") = 60000)
+        .def("capacity", &Server::capacity)
+        .def("stats", &Server::stats)
+        .def("close", &Server::close);
 }

@@ -252,7 +252,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
     __syncwarp();
     const int tlimit = (tsize >> 2) * 3;
 
-    int S = 0, lb = 0, nvis = 0, cmps = 0;
+    int S = 0, lb = 0, nvis = 0, cmps = 0, nexp = 0;
     bool overflow = false;
 
     // ---- initialize_search (graph.hpp:229-238) ----
@@ -342,6 +342,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         if (lane == 0) w.pid[f] = raw | kChecked;
         const int u = raw & kIdMask;
         lb = f + 1;
+        ++nexp;
         // adjacency row, stop at the first -1; skip repeats within the row and visited ids
         const int32_t *row = ix.adj + (size_t)u * (size_t)ix.K;
         int m = 0;
@@ -389,6 +390,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             bv.status[qi] = 1;
             atomicAdd(bv.overflow, 1u);
             if (bv.cmps) bv.cmps[qi] = cmps;
+            if (bv.expansions) bv.expansions[qi] = nexp;
         }
         __syncwarp();
         return;
@@ -421,9 +423,12 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             const float dj = rdis[j];
             const int32_t ij = rid[j];
             int rank = 0;
+            // (distance, id) order of Neighbor (neighbor.hpp:205-207); an id that entered the pool
+            // twice (a repeated entry point) keeps both copies, ordered by position
             for (int i = 0; i < avail; ++i) {
                 const float di = rdis[i];
-                rank += (di < dj) || (di == dj && rid[i] < ij);
+                const int32_t ii = rid[i];
+                rank += (di < dj) || (di == dj && (ii < ij || (ii == ij && i < j)));
             }
             if (rank < kq) {
                 oid[rank] = ij;
@@ -439,6 +444,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
     if (lane == 0) {
         bv.status[qi] = 0;
         if (bv.cmps) bv.cmps[qi] = cmps;
+        if (bv.expansions) bv.expansions[qi] = nexp;
     }
     __syncwarp();
 }
