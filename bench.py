@@ -201,10 +201,14 @@ def run_gpu(a):
     nq, d = queries.shape
     s = glass.Searcher(glass.Graph(GRAPH), base, "L2", "SQ4U", "FP32", device=local)
     s.set_ef(a.ef)
+    s.batch_search(queries, K)  # sizes the visited table from this workload's visit counts
     if not a.profile:
         s.optimize()
     tuning = s.get_tuning()
-    stream = torch.cuda.current_stream()
+    # a stream of our own: the legacy default stream has handle 0, which the C ABI reads as
+    # "the searcher's stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     dq = torch.from_numpy(queries).cuda()
     ids = torch.empty((nq, K), dtype=torch.int32, device="cuda")
     dis = torch.empty((nq, K), dtype=torch.float32, device="cuda")

@@ -132,11 +132,14 @@ int upload(DevBuf &b, const T *src, size_t n, cudaStream_t st) {
     return GSX_OK;
 }
 
+// Shared-memory visited-table size.  A query whose visited set outgrows it moves the set into its
+// warp's global spill table and continues (exact), so the size trades occupancy against the
+// share of queries that spill: it is sized for about twice the typical visit count (the mean
+// seen on this searcher, else ef*K/2), between 2^9 and 2^13 slots.
 int default_table_bits(const gsx_searcher *s, int efmax) {
-    // expected visits ~ ef * K; keep the table at most about half full
-    int64_t want = (int64_t)efmax * s->ix.K + 64;
-    int bits = kMinTableBits;
-    while ((1ll << bits) < want && bits < 30) ++bits;
+    int64_t want = s->visit_avg > 0 ? (int64_t)(2.0 * s->visit_avg) : (int64_t)efmax * s->ix.K / 2;
+    int bits = 9;
+    while ((1ll << bits) < want && bits < 13) ++bits;
     return bits;
 }
 
@@ -203,6 +206,12 @@ int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int3
     bv.status = s->status.as<int32_t>();
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
+    // one spill table per resident warp, 8x the shared table (at least 2^14 slots)
+    const int sbits = s->tuning.spill_bits > 0 ? s->tuning.spill_bits : std::min(16, std::max(14, cfg.L.table_bits + 3));
+    const size_t slots = (size_t)cfg.blocks * cfg.warps_per_block;
+    if ((rc = s->spill.ensure(slots * ((size_t)1 << sbits) * 4))) return rc;
+    bv.gtab = s->spill.as<int32_t>();
+    bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     return GSX_OK;
 }
@@ -306,6 +315,14 @@ int host_batch(gsx_searcher *s, const float *queries, int nq, int k, const int32
     s->h_cmps.resize((size_t)nq);
     GSX_CUDA(cudaMemcpyAsync(s->h_cmps.data(), s->cmps.p, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
     GSX_CUDA(cudaStreamSynchronize(st));
+    int32_t mx = 0;
+    int64_t sum = 0;
+    for (int i = 0; i < nq; ++i) {
+        mx = std::max(mx, s->h_cmps[i]);
+        sum += s->h_cmps[i];
+    }
+    s->visit_hint = std::max(s->visit_hint, mx);
+    if (nq >= 32) s->visit_avg = (double)sum / nq;
     if (!single) {
         // SearchBatch: average distance computations (graph_searcher.hpp:156-158)
         int64_t tot = 0;
@@ -500,7 +517,7 @@ void gsx_searcher_destroy(gsx_searcher *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->q, &s->ids,
                       &s->dis, &s->status, &s->cmps, &s->efp, &s->kp, &s->order, &s->counters, &s->gtab,
-                      &s->dist_out, &s->dist_ids})
+                      &s->spill, &s->dist_out, &s->dist_ids})
         b->release();
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -617,6 +634,8 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
         return fail(GSX_ERR_INVALID, "lanes_per_row must be 0, 1, 2 or 4");
     if (t->table_bits != 0 && (t->table_bits < kMinTableBits || t->table_bits > 16))
         return fail(GSX_ERR_INVALID, "table_bits must be 0 or in [%d, 16]", kMinTableBits);
+    if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
+        return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
     s->tuning = *t;
     if ((s->kind == K_E5M2 || s->kind == K_FP32) && s->tuning.lanes_per_row == 2) s->tuning.lanes_per_row = 4;
     return GSX_OK;
@@ -641,7 +660,7 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
     for (int wpb : {2, 4, 8})
         for (int lpr : lprs)
             for (int db : {-1, 0, 1}) {
-                gsx_tuning t{wpb, std::max(kMinTableBits, base_bits + db), lpr, saved.prefetch};
+                gsx_tuning t{wpb, std::max(kMinTableBits, base_bits + db), lpr, saved.prefetch, saved.spill_bits};
                 s->tuning = t;
                 float ms_min = 1e30f;
                 bool ok = true;

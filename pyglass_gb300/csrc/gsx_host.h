@@ -73,15 +73,17 @@ struct gsx_searcher {
     int num_sms = 0;
 
     // per-call scratch (device)
-    gsx::DevBuf q, ids, dis, status, cmps, efp, kp, order, counters, gtab, dist_out, dist_ids;
+    gsx::DevBuf q, ids, dis, status, cmps, efp, kp, order, counters, gtab, spill, dist_out, dist_ids;
     // host copies for reporting
     std::vector<int32_t> h_cmps, h_status;
     double last_avg_cmps = 0.0;
+    int32_t visit_hint = 0;  // largest per-query distance count seen
+    double visit_avg = 0.0;  // mean per-query distance count of the last large batch
 
     // sample of base rows kept for optimize (graph_searcher.hpp:62-69)
     std::vector<float> sample;
     int32_t sample_n = 0;
 
-    gsx_tuning tuning{0, 0, 0, 1};
+    gsx_tuning tuning{0, 0, 0, 1, 0};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };

@@ -98,6 +98,7 @@ struct gsx_server {
     std::vector<cudaStream_t> streams;
     std::vector<Group *> running;  // per stream
     DevBuf dq, dids, ddis, dk, def, dstatus, dorder, dcnt;
+    std::vector<std::unique_ptr<DevBuf>> spill;  // per stream: visited-set spill tables of the group's warps
     float *hq = nullptr;
     int32_t *hids = nullptr, *hk = nullptr, *hef = nullptr, *horder = nullptr, *hstatus = nullptr;
     float *hdis = nullptr;
@@ -192,6 +193,12 @@ int launch_group(gsx_server *sv, Group *g, int si) {
     bv.status = sv->dstatus.as<int32_t>();
     bv.counter = cnt;
     bv.overflow = cnt + 1;
+    const int sbits = sv->s->tuning.spill_bits > 0 ? sv->s->tuning.spill_bits
+                                                   : std::min(16, std::max(14, cfg.L.table_bits + 3));
+    DevBuf &sp = *sv->spill[si];
+    if ((rc = sp.ensure((size_t)cfg.blocks * cfg.warps_per_block * ((size_t)1 << sbits) * 4))) return rc;
+    bv.gtab = sp.as<int32_t>();
+    bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(sv->s->ix, bv, cfg, st));
     for (Request *r : g->reqs) {
         const size_t o = (size_t)r->slot0;
@@ -313,6 +320,7 @@ int gsx_server_create(gsx_searcher *s, int32_t max_queries_in_flight, int32_t km
         return bad(fail(GSX_ERR_NOMEM, "pinned host allocation failed"));
     sv->streams.resize(streams, nullptr);
     sv->running.assign(streams, nullptr);
+    for (int i = 0; i < streams; ++i) sv->spill.emplace_back(new DevBuf);
     for (auto &st : sv->streams) {
         cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
         if (e != cudaSuccess) return bad(cuda_fail(e, "cudaStreamCreate"));

@@ -245,10 +245,11 @@ struct Searcher {
         d["table_bits"] = t.table_bits;
         d["lanes_per_row"] = t.lanes_per_row;
         d["prefetch"] = t.prefetch;
+        d["spill_bits"] = t.spill_bits;
         return d;
     }
-    void set_tuning(int warps_per_block, int table_bits, int lanes_per_row, int prefetch) {
-        gsx_tuning t{warps_per_block, table_bits, lanes_per_row, prefetch};
+    void set_tuning(int warps_per_block, int table_bits, int lanes_per_row, int prefetch, int spill_bits) {
+        gsx_tuning t{warps_per_block, table_bits, lanes_per_row, prefetch, spill_bits};
         check(gsx_searcher_set_tuning(s, &t));
     }
     py::tuple memory() const {
@@ -357,7 +358,7 @@ PYBIND11_MODULE(_glass, m) {
         .def("calibration", &Searcher::calibration)
         .def("get_tuning", &Searcher::get_tuning)
         .def("set_tuning", &Searcher::set_tuning, py::arg("warps_per_block") = 0, py::arg("table_bits") = 0,
-             py::arg("lanes_per_row") = 0, py::arg("prefetch") = 1)
+             py::arg("lanes_per_row") = 0, py::arg("prefetch") = 1, py::arg("spill_bits") = 0)
         .def("memory", &Searcher::memory);
 
     py::class_<Server>(m, "Server")

@@ -70,15 +70,6 @@ __device__ __forceinline__ int upper_bound_u32(const uint32_t *a, int n, uint32_
     return lo;
 }
 
-__device__ __forceinline__ int count_le_i32(const int32_t *a, int n, int x) {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (a[mid] > x) hi = mid; else lo = mid + 1;
-    }
-    return lo;
-}
-
 struct WarpState {
     uint32_t *pkey;
     int32_t *pid;
@@ -91,13 +82,41 @@ struct WarpState {
     uint32_t *qc;
     int32_t *tab;
     int tbits;
+    int32_t *spill;  // this warp's global-memory table, used once the shared one is full
+    int sbits;
+    int32_t *tab0;   // the table every query starts with
+    int tbits0;
 };
+
+// Moves the visited set from the shared-memory table into the warp's global table (cleared
+// first) and continues there: the set is unchanged, only its storage grows.
+__device__ __forceinline__ void migrate_visited(WarpState &w, int lane) {
+    const int gsize = 1 << w.sbits;
+    for (int j = lane * 4; j < gsize; j += 128) *reinterpret_cast<int4 *>(w.spill + j) = make_int4(-1, -1, -1, -1);
+    __syncwarp();
+    __threadfence_block();
+    const int tsize = 1 << w.tbits;
+    for (int j = lane; j < tsize; j += 32) {
+        const int32_t v = w.tab[j];
+        if (v != -1) visit(w.spill, w.sbits, v);
+    }
+    __syncwarp();
+    w.tab = w.spill;
+    w.tbits = w.sbits;
+}
 
 // Merges candidates cand_{id,key}[0..m) (in insertion order, m <= 64) into the pool
 // pkey/pid[0..S) of capacity cap.  Exactly the state LinearPool::insert (neighbor.hpp:382-396)
 // reaches by inserting them one after the other: a candidate lands after every pool entry with
 // an equal or smaller key and after the earlier candidates with equal keys; entries pushed past
 // cap are dropped.  `lb` is a lower bound of the first unexpanded index and is updated.
+//
+// Candidate j's final slot is ub_j + rank_j (ub = upper bound in the pool, rank = position among
+// the candidates ordered by (key, arrival)); the accepted candidates are those whose slot is below
+// cap, i.e. the lowest ranks.  The pool is then rebuilt from the top in 32-slot chunks: a
+// redux.or of the candidates' slot bits in the chunk says which slots take a candidate, and every
+// other slot p takes the pool entry p - (candidates placed below p).  A chunk only reads entries
+// at or below its own slots, so no entry is overwritten before it is read.
 __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, int m, int lane) {
     int nacc = 0;
 #pragma unroll
@@ -127,36 +146,49 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     }
     __syncwarp();
     if (nacc == 0) return;
-    const int lo = w.acc_ub[0];
-    // shift pool entries [lo, S) to their new places, highest chunk first (no entry is read
-    // after its slot was written: destinations are >= sources and strictly increasing)
-    for (int top = S; top > lo; top -= 32) {
-        const int i = top - 1 - lane;
-        const bool act = i >= lo;
+    // slots of the accepted candidates, rank r held by lane r (and r+32)
+    constexpr int kNone = 0x7fffffff;
+    const int ub0 = lane < nacc ? w.acc_ub[lane] : kNone;
+    const int ub1 = lane + 32 < nacc ? w.acc_ub[lane + 32] : kNone;
+    const int p0 = ub0 == kNone ? kNone : ub0 + lane;
+    const int p1 = ub1 == kNone ? kNone : ub1 + lane + 32;
+    const int lo = __shfl_sync(kFull, p0, 0);  // slot of the rank-0 candidate = acc_ub[0]
+    const int newS = (S + m) < cap ? (S + m) : cap;
+    const unsigned ltm = (1u << lane) - 1u;
+    const int nchunks = (newS - lo + 31) >> 5;
+    for (int c = nchunks - 1; c >= 0; --c) {
+        const int base = lo + 32 * c;
+        const int below = __popc(__ballot_sync(kFull, p0 < base)) + __popc(__ballot_sync(kFull, p1 < base));
+        unsigned bits = 0;
+        if (p0 >= base && p0 < base + 32) bits |= 1u << (p0 - base);
+        if (p1 >= base && p1 < base + 32) bits |= 1u << (p1 - base);
+        const unsigned cm = __reduce_or_sync(kFull, bits);
+        const int p = base + lane;
+        const int r = below + __popc(cm & ltm);
         uint32_t k = 0;
         int32_t id = 0;
-        int np = 0;
-        if (act) {
-            k = w.pkey[i];
-            id = w.pid[i];
-            np = i + count_le_i32(w.acc_ub, nacc, i);
+        if (p < newS) {
+            if ((cm >> lane) & 1u) {
+                k = w.acc_key[r];
+                id = w.acc_id[r];
+            } else {
+                k = w.pkey[p - r];
+                id = w.pid[p - r];
+            }
         }
         __syncwarp();
-        if (act && np < cap) {
-            w.pkey[np] = k;
-            w.pid[np] = id;
+        if (p < newS) {
+            w.pkey[p] = k;
+            w.pid[p] = id;
         }
         __syncwarp();
     }
-    for (int r = lane; r < nacc; r += 32) {
-        const int p = w.acc_ub[r] + r;
-        w.pkey[p] = w.acc_key[r];
-        w.pid[p] = w.acc_id[r];
-    }
-    const int sl = count_le_i32(w.acc_ub, nacc, lb);
+    // new lower bound of the first unexpanded entry: the first candidate, or where the old bound
+    // moved to
+    const int sl = __popc(__ballot_sync(kFull, ub0 <= lb)) + __popc(__ballot_sync(kFull, ub1 <= lb));
     const int nl = lb + sl;
     lb = lo < nl ? lo : nl;
-    S = (S + m) < cap ? (S + m) : cap;
+    S = newS;
     __syncwarp();
 }
 
@@ -246,11 +278,13 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
     __syncwarp();
     const int32_t qsq = prepare_query<KIND, METRIC>(ix, w, lane);
 
-    // visited table reset
+    // visited table reset (back to the shared-memory table if the last query spilled)
+    w.tab = w.tab0;
+    w.tbits = w.tbits0;
     const int tsize = 1 << w.tbits;
     for (int j = lane * 4; j < tsize; j += 128) *reinterpret_cast<int4 *>(w.tab + j) = make_int4(-1, -1, -1, -1);
     __syncwarp();
-    const int tlimit = (tsize >> 2) * 3;
+    int tlimit = (tsize >> 2) * 3;
 
     int S = 0, lb = 0, nvis = 0, cmps = 0, nexp = 0;
     bool overflow = false;
@@ -336,7 +370,13 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
     while (!overflow) {
         const int f = first_unchecked(w.pid, lb, S < lim ? S : lim, lane);
         if (f >= S || f >= lim) break;
-        if (nvis + ix.K > tlimit) { overflow = true; break; }
+        if (nvis + ix.K > tlimit) {
+            if (w.spill && w.tab != w.spill) {
+                migrate_visited(w, lane);
+                tlimit = ((1 << w.tbits) >> 2) * 3;
+            }
+            if (nvis + ix.K > tlimit) { overflow = true; break; }
+        }
         const int32_t raw = w.pid[f];
         __syncwarp();
         if (lane == 0) w.pid[f] = raw | kChecked;
@@ -465,14 +505,18 @@ __global__ void __launch_bounds__(256) search_kernel(IndexView ix, BatchView bv,
     w.acc_id = reinterpret_cast<int32_t *>(ws + L.acc_id);
     w.fq = reinterpret_cast<float *>(ws + L.fq);
     w.qc = reinterpret_cast<uint32_t *>(ws + L.qc);
+    const size_t slot = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    w.spill = bv.gtab ? bv.gtab + (slot << bv.gtab_bits) : nullptr;
+    w.sbits = bv.gtab_bits;
     if (L.table_bits > 0) {
-        w.tab = reinterpret_cast<int32_t *>(ws + L.table);
-        w.tbits = L.table_bits;
+        w.tab0 = reinterpret_cast<int32_t *>(ws + L.table);
+        w.tbits0 = L.table_bits;
     } else {
-        const size_t slot = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
-        w.tab = bv.gtab + (slot << bv.gtab_bits);
-        w.tbits = bv.gtab_bits;
+        w.tab0 = w.spill;
+        w.tbits0 = bv.gtab_bits;
     }
+    w.tab = w.tab0;
+    w.tbits = w.tbits0;
     while (true) {
         unsigned t = 0;
         if (lane == 0) t = atomicAdd(bv.counter, 1u);

@@ -73,6 +73,16 @@ WORKLOADS = {
                        index=("NSG", 32, 50, "SQ8U"), metric="L2",
                        desc="1,000,000 x 128 from 1,024 clusters (sigma 12, integers 0..255), NSG R=32 L=50 "
                             "(build quant SQ8U), 10,000 queries"),
+    # reduced-size versions of the 960-d low-rank (HNSW R=32 L=200) and 768-d normalised (NSG
+    # R=48 L=100, inner product) workloads, used as parity cases
+    "lowrank100k": dict(base=lambda: low_rank(100_000, 960, seed=3), queries=lambda: low_rank(1_000, 960, seed=3, stream=1),
+                        index=("HNSW", 32, 200, "SQ8U"), metric="L2",
+                        desc="100,000 x 960 low-rank (x = Wz + e, rank 32, noise 0.05), HNSW R=32 L=200, 1,000 queries"),
+    "sphere200k": dict(base=lambda: normalized_mixture(200_000, 768, seed=4),
+                       queries=lambda: normalized_mixture(2_000, 768, seed=4, stream=1),
+                       index=("NSG", 48, 100, "SQ8U"), metric="IP",
+                       desc="200,000 x 768 unit vectors from 4,096 clusters (sigma 0.3), NSG R=48 L=100 (L2 build), "
+                            "2,000 queries, inner product"),
 }
 
 

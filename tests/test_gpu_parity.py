@@ -109,12 +109,16 @@ def test_mixed_ef_and_k(gpu, oracle):
     np.testing.assert_array_equal(gd, od)
 
 
-def test_visited_table_overflow_is_retried_exactly(gpu, oracle):
+@pytest.mark.parametrize("spill_bits", [0, 7])
+def test_visited_table_overflow_is_exact(gpu, oracle, spill_bits):
+    """A 128-slot shared table (96 visits) overflows: the visited set moves to the warp's global
+    spill table and the search goes on; with a 128-slot spill table too, the query is re-run by the
+    host with a table sized for the whole graph.  Either way the results are exact."""
     s = searcher(gpu, "nsg_d100", "SQ8U", "L2")
     o = oracle.Searcher(oracle.Graph(os.path.join(GOLDEN_DIR, "nsg_d100.glass")), spec.base(), "L2", "SQ8U")
     q = spec.queries()
     try:
-        s.set_tuning(warps_per_block=4, table_bits=7, lanes_per_row=1, prefetch=1)  # 96 visits max
+        s.set_tuning(warps_per_block=4, table_bits=7, lanes_per_row=1, prefetch=1, spill_bits=spill_bits)
         s.set_ef(64)
         o.set_ef(64)
         gi, gd = s.batch_search(q, 10)
@@ -123,7 +127,7 @@ def test_visited_table_overflow_is_retried_exactly(gpu, oracle):
         np.testing.assert_array_equal(gd, od)
         assert s.get_last_search_dist_cmps() == o.get_last_search_dist_cmps()
     finally:
-        s.set_tuning(0, 0, 0, 1)
+        s.set_tuning(0, 0, 0, 1, 0)
 
 
 def test_tuning_variants_agree(gpu, golden):
@@ -135,12 +139,12 @@ def test_tuning_variants_agree(gpu, golden):
         for wpb in (1, 2, 8):
             for lpr in (1, 2, 4):
                 for prefetch in (0, 1):
-                    s.set_tuning(warps_per_block=wpb, table_bits=0, lanes_per_row=lpr, prefetch=prefetch)
+                    s.set_tuning(warps_per_block=wpb, table_bits=0, lanes_per_row=lpr, prefetch=prefetch, spill_bits=0)
                     ids, dis = s.batch_search(q, 10)
                     np.testing.assert_array_equal(ids, ref_ids)
                     np.testing.assert_array_equal(dis, ref_dis)
     finally:
-        s.set_tuning(0, 0, 0, 1)
+        s.set_tuning(0, 0, 0, 1, 0)
 
 
 def test_optimize_keeps_results(gpu):
@@ -154,7 +158,7 @@ def test_optimize_keeps_results(gpu):
     b = s.batch_search(q, 10)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
-    s.set_tuning(0, 0, 0, 1)
+    s.set_tuning(0, 0, 0, 1, 0)
 
 
 def test_edge_inputs(gpu):
