@@ -108,6 +108,22 @@ int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, in
  * (synchronises the searcher's stream). */
 int gsx_searcher_overflow_count(gsx_searcher *s, uint32_t *count);
 
+/* Allocation-free batched search; no counterpart in the reference.  For callers that may not
+ * allocate device memory while they serve: engines that hand all GPU memory to their own pool at
+ * start-up, and latency-bound paths that cannot take the device-wide synchronisation an allocation
+ * or free can cause.  The call allocates nothing: d_queries (nq x dim fp32) and d_ids / d_dis
+ * (nq x k) are the caller's device buffers, and the per-call scratch (work-queue counters and one
+ * status word per query) is a fixed array inside the library, about 256 KB on every GPU that loads
+ * it, held until the process exits.  Hence at most 65,536 queries per call; a larger nq is
+ * rejected with GSX_ERR_INVALID.  The first call on a device looks up that array's device address;
+ * make it before any stream capture.  All calls share the array and it keeps the last call's
+ * contents: calls that overlap on the GPU (other streams or threads) race, so the caller must
+ * serialise them.  Enqueued on `stream` (NULL = the searcher's stream) with the searcher's ef,
+ * without synchronising.  A query whose visited set outgrows its shared-memory table is left
+ * unanswered (all its k ids are -1); the allocating entry points answer every query. */
+int gsx_searcher_search_batch_noalloc(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
+                                      int32_t *d_ids, float *d_dis, void *stream);
+
 /* Same as above with HOST buffers (copies inside), synchronous. */
 int gsx_searcher_search_batch_mixed(gsx_searcher *s, const float *queries, int32_t nq, int32_t k,
                                     const int32_t *ef, const int32_t *kq, int32_t kmax, int32_t *ids, float *dis);

@@ -334,6 +334,12 @@ int host_batch(gsx_searcher *s, const float *queries, int nq, int k, const int32
 
 }  // namespace
 
+// Launch configuration of the allocation-free search (noalloc.cu): no spill tables exist there, so
+// the shared-memory visited table is the largest default (2^13 slots) unless tuned.
+int noalloc_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg) {
+    return make_cfg(s, kmax, efmax, nq, false, s->tuning.table_bits > 0 ? s->tuning.table_bits : 13, cfg);
+}
+
 // Hooks of the serving loop (gsx_server.cpp).
 int server_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg) {
     return make_cfg(s, kmax, efmax, nq, false, 0, cfg);
