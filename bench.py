@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "QPS at recall@10>=0.95 (1M×128, SQ4U), batched/served vs plain; p50/p99 latency"
 WORKLOAD = "clusters1m"
-GRAPH = os.path.join(ROOT, "data", f"{WORKLOAD}.glass")
+META = os.path.join(ROOT, "data", f"{WORKLOAD}.json")
 SWEEP_EF = [16, 32, 64, 128]
 K = 10
 
@@ -48,12 +48,34 @@ def args_():
     return p.parse_args()
 
 
+def graph_file():
+    from pyglass_gb300 import datasets
+
+    found = datasets.graph_file(WORKLOAD, ROOT)
+    if found is None:
+        raise SystemExit(json.dumps({"error": f"data/{WORKLOAD}.glass missing: run python oracle/build_graphs.py {WORKLOAD}"}))
+    return found
+
+
+def glass_path():
+    """A glass-format copy of the graph (the CPU searcher reads only that format)."""
+    path, fmt = graph_file()
+    if fmt == "glass":
+        return path
+    import tempfile
+
+    from pyglass_gb300 import glass
+
+    tmp = os.path.join(tempfile.mkdtemp(), f"{WORKLOAD}.glass")
+    glass.Graph(path, fmt).save(tmp)
+    return tmp
+
+
 def load_workload():
     from pyglass_gb300 import datasets
 
-    if not os.path.exists(GRAPH):
-        raise SystemExit(json.dumps({"error": f"{GRAPH} missing: run python oracle/build_graphs.py {WORKLOAD}"}))
-    meta = json.load(open(GRAPH.replace(".glass", ".json")))
+    graph_file()
+    meta = json.load(open(META))
     w = datasets.WORKLOADS[WORKLOAD]
     base, queries = w["base"](), w["queries"]()
     if datasets.checksum(base) != meta["base_checksum"]:
@@ -76,7 +98,7 @@ def cpu_baseline(base, queries, ef, sample):
     from oracle import pyoracle
 
     pyoracle.build(ref=False)
-    g = pyoracle.Graph(GRAPH)
+    g = pyoracle.Graph(glass_path())
     s = pyoracle.Searcher(g, base, "L2", "SQ4U", "FP32")
     s.set_ef(ef)
     q = queries[:sample]
@@ -134,18 +156,51 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def ground_truth(torch, base_t, q_t, k):
-    """Exact k nearest neighbours (fp32; the data are integers, so the products are exact)."""
-    xn = (base_t * base_t).sum(1)
-    out = []
-    for s in range(0, q_t.shape[0], 500):
-        d = xn[None, :] - 2.0 * (q_t[s:s + 500] @ base_t.T)
-        out.append(torch.topk(d, k, dim=1, largest=False).indices.int())
-    return torch.cat(out).cpu().numpy()
+def ground_truth(torch, glass, base_t, q_t, k):
+    """Exact k nearest neighbours from the tensor-core kernel (gsx_knn_exact), spot-checked against
+    a float64 CPU recompute on 20 queries."""
+    ids = torch.empty((q_t.shape[0], k), dtype=torch.int32, device="cuda")
+    dis = torch.empty((q_t.shape[0], k), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    exact = glass.knn_exact(base_t.data_ptr(), base_t.shape[0], base_t.shape[1], q_t.data_ptr(), q_t.shape[0], k,
+                            False, ids.data_ptr(), dis.data_ptr())
+    gt, gd = ids.cpu().numpy(), dis.cpu().numpy()
+    b = base_t.cpu().numpy().astype(np.float64)
+    q = q_t[:20].cpu().numpy().astype(np.float64)
+    ok = True
+    for i in range(20):
+        d = ((b - q[i]) ** 2).sum(1)
+        kth = np.partition(d, k - 1)[k - 1]
+        ok &= bool(np.allclose(np.sort(d[gt[i]]), np.sort(d)[:k]) and d[gt[i]].max() <= kth)
+    return gt, {"kernel": "tcgen05 bf16 (single exact pass)" if exact else "tcgen05 bf16 hi/lo split",
+                "cpu_recheck_20_queries": ok}
 
 
 def recall(ids, gt):
     return float(np.mean([len(np.intersect1d(ids[i, :K], gt[i, :K])) for i in range(ids.shape[0])])) / K
+
+
+def serving_leg(glass, s, queries):
+    """Continuous batching under an open-loop Poisson stream: requests of 1..256 queries
+    (log-uniform), k in {10, 100}, ef in {32, 64, 128, 256}; the saturation throughput is measured
+    with a burst, then p50/p99 request latency at 10%, 50% and 90% of it."""
+    srv = glass.Server(s, capacity=16384, kmax=100, efmax=256, streams=4)
+    ks, efs = [10, 100], [32, 64, 128, 256]
+    mean_size = 256 / np.log(257) - 0.5
+    lat, sz, wall = srv.drive_poisson(queries, 2000, 1e7, 1, 256, ks, efs, 7)  # burst: saturation
+    sat_qps = float(sz.sum() / wall)
+    points = []
+    for frac in (0.1, 0.5, 0.9):
+        qps = frac * sat_qps
+        rate = qps / mean_size
+        n = int(min(30000, max(300, rate * 2.5)))
+        lat, sz, wall = srv.drive_poisson(queries, n, rate, 1, 256, ks, efs, 11)
+        points.append({"offered_qps": qps, "achieved_qps": float(sz.sum() / wall), "requests": n,
+                       "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
+    srv.close()
+    return {"saturation_qps": sat_qps, "mix": "1..256 queries/request (log-uniform), k {10,100}, ef {32,64,128,256}",
+            "points": points, "p50_ms": points[1]["p50_ms"], "p99_ms": points[1]["p99_ms"],
+            "at": "50% of saturation"}
 
 
 def measured_peak():
@@ -199,7 +254,7 @@ def run_gpu(a):
 
     base, queries, meta = load_workload()
     nq, d = queries.shape
-    s = glass.Searcher(glass.Graph(GRAPH), base, "L2", "SQ4U", "FP32", device=local)
+    s = glass.Searcher(glass.Graph(*graph_file()), base, "L2", "SQ4U", "FP32", device=local)
     s.set_ef(a.ef)
     s.batch_search(queries, K)  # sizes the visited table from this workload's visit counts
     if not a.profile:
@@ -266,7 +321,7 @@ def run_gpu(a):
 
     out_ids = ids.cpu().numpy()
     base_t = torch.from_numpy(base).cuda()
-    gt = ground_truth(torch, base_t, dq, K)
+    gt, gt_info = ground_truth(torch, glass, base_t, dq, K)
     del base_t
     rec = recall(out_ids, gt)
 
@@ -309,6 +364,8 @@ def run_gpu(a):
     plain = {"qps": 1000.0 / float(lat_ms.mean()), "p50_ms": float(np.percentile(lat_ms, 50)),
              "p99_ms": float(np.percentile(lat_ms, 99)), "queries": int(lat_ms.size)}
 
+    serving = serving_leg(glass, s, queries)
+
     if rank == 0:
         cb, _ = cpu_baseline(base, queries, a.ef, min(a.cpu_sample, nq))
         line = {
@@ -324,6 +381,7 @@ def run_gpu(a):
                          "avg_expansions": float(x.mean())},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": a.steps, "clocks": clk.summary(),
             "plain_per_query": plain, "batched_over_plain": value / world / plain["qps"], "sweep": sweep,
+            "ground_truth": gt_info, "serving": serving,
         }
         print(json.dumps(line))
     if dist:

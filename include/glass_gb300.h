@@ -140,7 +140,8 @@ int gsx_searcher_get_last_search_avg_dist_cmps(const gsx_searcher *s, double *ou
 /* Tuning knobs chosen by gsx_searcher_optimize (0 = automatic). */
 typedef struct {
     int32_t warps_per_block;  /* queries per CTA */
-    int32_t table_bits;       /* log2 of the per-query visited-table slots in shared memory */
+    int32_t table_bits;       /* log2 of the per-query visited-table slots in shared memory
+                                 (1 = none: the visited set lives in the warp's global table) */
     int32_t lanes_per_row;    /* lanes cooperating on one code row (SQ kinds) */
     int32_t prefetch;         /* L2 prefetch of adjacency rows of accepted candidates */
     int32_t spill_bits;       /* log2 of the per-warp global table a full shared table spills into */
@@ -162,6 +163,17 @@ int gsx_searcher_distances(gsx_searcher *s, const float *queries, int32_t nq, co
 /* Copies out the encoded base rows (n*code_size bytes) and calibrator parameters (2 floats). */
 int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int32_t *code_size);
 
+/* ---- exact ground truth (no reference counterpart; replaces brute force in examples/main.py) -- */
+
+/* Exact k nearest neighbours of nq queries over N base rows by brute force on the tensor cores,
+ * for recall checks: bf16 tensor-core scores (one pass when every input is exactly representable
+ * in bf16, else a three-pass hi/lo split), 32 candidates per query per base chunk, then exact fp64
+ * rescoring; ids/dis are nq x k sorted by (distance, id).  Device buffers (fp32, row-major);
+ * d <= 128, k <= 16; ip = 1 for inner product (distance -q.x), else squared L2.  *exact_inputs (may
+ * be NULL) reports whether the single exact pass was used.  Synchronises `stream`. */
+int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k,
+                  int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream);
+
 /* ---- serving: continuous batching over a resident index (no reference counterpart) -------- */
 
 typedef struct gsx_server gsx_server;
@@ -182,6 +194,16 @@ int gsx_server_submit(gsx_server *sv, const float *queries, int32_t nq, int32_t 
 int gsx_server_wait(gsx_server *sv, uint64_t ticket, int32_t timeout_ms, int32_t *ids, float *dis, double *latency_ms);
 /* Completed queries, queued requests, groups on the device. */
 int gsx_server_stats(gsx_server *sv, int64_t *completed_queries, int32_t *queued_requests, int32_t *running_groups);
+/* Open-loop Poisson load for measuring a server (no reference counterpart): n_requests requests
+ * arrive at exponential gaps of mean 1/request_rate s; each has a log-uniform number of queries in
+ * [size_min, size_max] (consecutive rows of `queries`, nq_pool rows), a k drawn from ks[0..nk) and
+ * an ef from efs[0..nef).  Requests are submitted on schedule whether or not earlier ones have
+ * finished.  Writes every request's submit-to-completion latency (ms), its size (may be NULL) and
+ * the wall time of the whole run. */
+int gsx_server_drive_poisson(gsx_server *sv, const float *queries, int32_t nq_pool, int32_t n_requests,
+                             double request_rate, int32_t size_min, int32_t size_max, const int32_t *ks, int32_t nk,
+                             const int32_t *efs, int32_t nef, uint64_t seed, double *latency_ms, int32_t *sizes,
+                             double *wall_s);
 /* Finishes every queued request, then stops the loop and frees its memory. */
 void gsx_server_destroy(gsx_server *sv);
 

@@ -54,6 +54,20 @@ void DevBuf::release() {
     bytes = 0;
 }
 
+int SpillTables::ensure(size_t n, int b, cudaStream_t st, unsigned long long **tab, uint32_t **epoch) {
+    const size_t tbytes = n * ((size_t)1 << b) * 8;
+    if (!buf.p || n != slots || b != bits) {
+        int rc = buf.ensure(tbytes + n * 4);
+        if (rc) return rc;
+        GSX_CUDA(cudaMemsetAsync(buf.p, 0, tbytes + n * 4, st));
+        slots = n;
+        bits = b;
+    }
+    *tab = buf.as<unsigned long long>();
+    *epoch = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(buf.p) + tbytes);
+    return GSX_OK;
+}
+
 namespace {
 
 // quantizer_map (glass/quant/quant.hpp:25-43); operator[] on an unknown key yields FP32.
@@ -137,7 +151,7 @@ int upload(DevBuf &b, const T *src, size_t n, cudaStream_t st) {
 // share of queries that spill: it is sized for about twice the typical visit count (the mean
 // seen on this searcher, else ef*K/2), between 2^9 and 2^13 slots.
 int default_table_bits(const gsx_searcher *s, int efmax) {
-    int64_t want = s->visit_avg > 0 ? (int64_t)(2.0 * s->visit_avg) : (int64_t)efmax * s->ix.K / 2;
+    int64_t want = s->visit_avg > 0 ? (int64_t)(1.5 * s->visit_avg) : (int64_t)efmax * s->ix.K / 2;
     int bits = 9;
     while ((1ll << bits) < want && bits < 13) ++bits;
     return bits;
@@ -158,11 +172,16 @@ int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int tabl
     int lpr = s->tuning.lanes_per_row > 0 ? s->tuning.lanes_per_row
               : ((s->kind == K_E5M2 || s->kind == K_FP32) ? 4 : (s->ix.csize > 256 ? 4 : 1));
     WarpLayout L;
-    // shrink the table (down to the minimum) until one warp's slice fits; beyond that the
-    // global-memory table path is used
-    while (!make_layout(s->ix, cap, bits, s->tuning.prefetch, &L) && bits > kMinTableBits) --bits;
-    if (!make_layout(s->ix, cap, bits, s->tuning.prefetch, &L))
-        return fail(GSX_ERR_UNSUPPORTED, "per-query state does not fit in shared memory");
+    if (bits == kGlobalOnly) {
+        // no shared-memory table: every query keeps its visited set in its warp's global table
+        if (!make_layout(s->ix, cap, 0, s->tuning.prefetch, &L))
+            return fail(GSX_ERR_UNSUPPORTED, "per-query state does not fit in shared memory");
+    } else {
+        // shrink the table (down to the minimum) until one warp's slice fits
+        while (!make_layout(s->ix, cap, bits, s->tuning.prefetch, &L) && bits > kMinTableBits) --bits;
+        if (!make_layout(s->ix, cap, bits, s->tuning.prefetch, &L))
+            return fail(GSX_ERR_UNSUPPORTED, "per-query state does not fit in shared memory");
+    }
     while (wpb > 1 && (size_t)wpb * L.total > 227 * 1024) wpb >>= 1;
     cfg->warps_per_block = wpb;
     cfg->lanes_per_row = lpr;
@@ -170,8 +189,19 @@ int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int tabl
     int per_sm = search_max_blocks_per_sm(s->ix, *cfg);
     if (per_sm < 1) per_sm = 1;
     const int want = (nq + wpb - 1) / wpb;
-    cfg->blocks = std::max(1, std::min(want, per_sm * s->num_sms));
+    cfg->max_blocks = per_sm * s->num_sms;
+    cfg->blocks = std::max(1, std::min(want, cfg->max_blocks));
     return GSX_OK;
+}
+
+// Global (spill) table size: room for the largest visit count seen on this searcher at a 3/4 load
+// (2^12..2^16 slots), else 4x the shared table.
+int spill_bits_for(const gsx_searcher *s, const LaunchCfg &cfg) {
+    if (s->tuning.spill_bits > 0) return s->tuning.spill_bits;
+    int bits = 12;
+    const int64_t want = s->visit_hint > 0 ? (int64_t)s->visit_hint * 4 / 3 + 2 * s->ix.K : (int64_t)1 << (cfg.L.table_bits + 2);
+    while ((1ll << bits) < want && bits < 16) ++bits;
+    return bits;
 }
 
 // Enqueues one batch on `st`; nothing is synchronised.
@@ -206,11 +236,10 @@ int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int3
     bv.status = s->status.as<int32_t>();
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
-    // one spill table per resident warp, 8x the shared table (at least 2^14 slots)
-    const int sbits = s->tuning.spill_bits > 0 ? s->tuning.spill_bits : std::min(16, std::max(14, cfg.L.table_bits + 3));
-    const size_t slots = (size_t)cfg.blocks * cfg.warps_per_block;
-    if ((rc = s->spill.ensure(slots * ((size_t)1 << sbits) * 4))) return rc;
-    bv.gtab = s->spill.as<int32_t>();
+    // one spill table per resident warp of this launch shape, 4x the shared table (>= 2^13 slots)
+    const int sbits = spill_bits_for(s, cfg);
+    const size_t slots = (size_t)cfg.max_blocks * cfg.warps_per_block;
+    if ((rc = s->spill.ensure(slots, sbits, st, &bv.gtab, &bv.gtab_epoch))) return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     return GSX_OK;
@@ -241,7 +270,9 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     const int slots_max = 64;
     cfg.blocks = std::max(1, std::min(((int)redo.size() + 3) / 4, slots_max / 4));
     const size_t slots = (size_t)cfg.blocks * cfg.warps_per_block;
-    if ((rc = s->gtab.ensure(slots * ((size_t)1 << gbits) * 4))) return rc;
+    unsigned long long *gt = nullptr;
+    uint32_t *ge = nullptr;
+    if ((rc = s->gtab.ensure(slots, gbits, st, &gt, &ge))) return rc;
     if ((rc = upload(s->order, redo.data(), redo.size(), st))) return rc;
     if ((rc = s->status.ensure((size_t)nq * 4))) return rc;
     GSX_CUDA(cudaMemsetAsync(s->counters.p, 0, 8, st));
@@ -261,7 +292,8 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     bv.status = s->status.as<int32_t>();
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
-    bv.gtab = s->gtab.as<int32_t>();
+    bv.gtab = gt;
+    bv.gtab_epoch = ge;
     bv.gtab_bits = gbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     GSX_CUDA(cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
@@ -337,12 +369,15 @@ int host_batch(gsx_searcher *s, const float *queries, int nq, int k, const int32
 // Launch configuration of the allocation-free search (noalloc.cu): no spill tables exist there, so
 // the shared-memory visited table is the largest default (2^13 slots) unless tuned.
 int noalloc_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg) {
-    return make_cfg(s, kmax, efmax, nq, false, s->tuning.table_bits > 0 ? s->tuning.table_bits : 13, cfg);
+    const int tb = s->tuning.table_bits >= kMinTableBits ? s->tuning.table_bits : 13;
+    return make_cfg(s, kmax, efmax, nq, false, tb, cfg);
 }
 
 // Hooks of the serving loop (gsx_server.cpp).
-int server_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg) {
-    return make_cfg(s, kmax, efmax, nq, false, 0, cfg);
+int server_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg, int *spill_bits) {
+    const int rc = make_cfg(s, kmax, efmax, nq, false, 0, cfg);
+    *spill_bits = spill_bits_for(s, *cfg);
+    return rc;
 }
 
 int server_resolve_one(gsx_searcher *s, const float *q, int k, int ef, int32_t *ids, float *dis) {
@@ -522,8 +557,8 @@ void gsx_searcher_destroy(gsx_searcher *s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->q, &s->ids,
-                      &s->dis, &s->status, &s->cmps, &s->efp, &s->kp, &s->order, &s->counters, &s->gtab,
-                      &s->spill, &s->dist_out, &s->dist_ids})
+                      &s->dis, &s->status, &s->cmps, &s->efp, &s->kp, &s->order, &s->counters, &s->gtab.buf,
+                      &s->spill.buf, &s->dist_out, &s->dist_ids})
         b->release();
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -638,8 +673,9 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
         return fail(GSX_ERR_INVALID, "warps_per_block must be 0 or a power of two <= 8");
     if (t->lanes_per_row != 0 && t->lanes_per_row != 1 && t->lanes_per_row != 2 && t->lanes_per_row != 4)
         return fail(GSX_ERR_INVALID, "lanes_per_row must be 0, 1, 2 or 4");
-    if (t->table_bits != 0 && (t->table_bits < kMinTableBits || t->table_bits > 16))
-        return fail(GSX_ERR_INVALID, "table_bits must be 0 or in [%d, 16]", kMinTableBits);
+    if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
+        return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
+                    kMinTableBits);
     if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
         return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
     s->tuning = *t;
@@ -653,9 +689,15 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
     if (!s->has_data) return fail(GSX_ERR_STATE, "optimize before set_data");
     int rc = set_device(s);
     if (rc) return rc;
-    const int nq = s->sample_n, k = 10, d = s->ix.d;
+    // the sample is tiled to enough queries to fill the GPU several times over, so that the timing
+    // measures throughput (a single wave would only measure the slowest query's latency)
+    const int reps = std::max(1, (16384 + s->sample_n - 1) / s->sample_n);
+    const int nq = s->sample_n * reps, k = 10, d = s->ix.d;
     cudaStream_t st = s->stream;
-    if ((rc = upload(s->q, s->sample.data(), (size_t)nq * d, st))) return rc;
+    std::vector<float> tiled((size_t)nq * d);
+    for (int r = 0; r < reps; ++r)
+        std::memcpy(tiled.data() + (size_t)r * s->sample_n * d, s->sample.data(), (size_t)s->sample_n * d * 4);
+    if ((rc = upload(s->q, tiled.data(), (size_t)nq * d, st))) return rc;
     if ((rc = s->ids.ensure((size_t)nq * k * 4))) return rc;
     if ((rc = s->dis.ensure((size_t)nq * k * 4))) return rc;
     const gsx_tuning saved = s->tuning;
@@ -663,10 +705,13 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
     std::vector<int> lprs = (s->kind == K_E5M2 || s->kind == K_FP32) ? std::vector<int>{1, 4} : std::vector<int>{1, 2, 4};
     gsx_tuning best = saved;
     float best_ms = 1e30f;
-    for (int wpb : {2, 4, 8})
+    // shared tables from 2^8 slots up to the default size, and none at all (global table only)
+    std::vector<int> bit_choices{kGlobalOnly};
+    for (int b = 8; b <= std::max(8, base_bits); ++b) bit_choices.push_back(b);
+    for (int wpb : {1, 2, 4})
         for (int lpr : lprs)
-            for (int db : {-1, 0, 1}) {
-                gsx_tuning t{wpb, std::max(kMinTableBits, base_bits + db), lpr, saved.prefetch, saved.spill_bits};
+            for (int bits : bit_choices) {
+                gsx_tuning t{wpb, bits, lpr, saved.prefetch, saved.spill_bits};
                 s->tuning = t;
                 float ms_min = 1e30f;
                 bool ok = true;

@@ -39,6 +39,10 @@ int graph_save(const HostGraph &g, const char *path);
 int validate_graph(const HostGraph &g);
 
 // A device allocation that grows on demand.
+struct DevBuf;
+// Spill tables of `slots` warps (2^bits 64-bit entries each) followed by their epoch counters;
+// zeroed whenever the layout changes, so every slot reads as empty and epochs restart.
+struct SpillTables;
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
@@ -47,6 +51,13 @@ struct DevBuf {
     ~DevBuf() { release(); }
     template <typename T>
     T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct SpillTables {
+    DevBuf buf;
+    size_t slots = 0;
+    int bits = 0;
+    int ensure(size_t slots, int bits, cudaStream_t st, unsigned long long **tab, uint32_t **epoch);
 };
 
 }  // namespace gsx
@@ -73,7 +84,8 @@ struct gsx_searcher {
     int num_sms = 0;
 
     // per-call scratch (device)
-    gsx::DevBuf q, ids, dis, status, cmps, efp, kp, order, counters, gtab, spill, dist_out, dist_ids;
+    gsx::DevBuf q, ids, dis, status, cmps, efp, kp, order, counters, dist_out, dist_ids;
+    gsx::SpillTables spill, gtab;  // per-warp spill tables; whole-graph tables of the exact re-run
     // host copies for reporting
     std::vector<int32_t> h_cmps, h_status;
     double last_avg_cmps = 0.0;

@@ -14,6 +14,7 @@ enum MetricId : int { M_L2 = 0, M_IP = 1 };
 constexpr int kMaxDegree = 64;       // graph degree handled per row (two 32-wide chunks)
 constexpr int kMaxCap = 1024;        // largest pool capacity max(k*factor, ef)
 constexpr int kMinTableBits = 7;     // smallest visited table: 128 slots
+constexpr int kGlobalOnly = 1;       // table_bits value: no shared table, visited set in global memory
 
 // Device-resident index, as the kernels see it.
 struct IndexView {
@@ -51,7 +52,8 @@ struct BatchView {
     int32_t *status;          // per-query: 0 ok, 1 visited table full (query left unanswered)
     unsigned int *counter;    // work-queue head, zeroed before the launch
     unsigned int *overflow;   // number of overflowed queries
-    int32_t *gtab;            // optional global visited tables, one slot per warp
+    unsigned long long *gtab; // optional global visited tables (epoch << 32 | id), one per warp slot
+    uint32_t *gtab_epoch;     // their epoch counters (zero-initialised)
     int32_t gtab_bits;
 };
 
@@ -69,6 +71,7 @@ struct LaunchCfg {
     int warps_per_block;
     int lanes_per_row;
     int blocks;
+    int max_blocks;           // resident blocks of this shape on the whole GPU (spill slots / warps)
     WarpLayout L;
 };
 

@@ -21,12 +21,14 @@
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <cmath>
+#include <random>
 #include <vector>
 
 #include "gsx_host.h"
 
 namespace gsx {
-int server_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg);
+int server_make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, LaunchCfg *cfg, int *spill_bits);
 int server_resolve_one(gsx_searcher *s, const float *q, int k, int ef, int32_t *ids, float *dis);
 }  // namespace gsx
 
@@ -98,7 +100,7 @@ struct gsx_server {
     std::vector<cudaStream_t> streams;
     std::vector<Group *> running;  // per stream
     DevBuf dq, dids, ddis, dk, def, dstatus, dorder, dcnt;
-    std::vector<std::unique_ptr<DevBuf>> spill;  // per stream: visited-set spill tables of the group's warps
+    std::vector<std::unique_ptr<SpillTables>> spill;  // per stream: visited-set spill tables of the group's warps
     float *hq = nullptr;
     int32_t *hids = nullptr, *hk = nullptr, *hef = nullptr, *horder = nullptr, *hstatus = nullptr;
     float *hdis = nullptr;
@@ -177,7 +179,8 @@ int launch_group(gsx_server *sv, Group *g, int si) {
     unsigned *cnt = sv->dcnt.as<unsigned>() + 2 * si;
     GSX_CUDA(cudaMemsetAsync(cnt, 0, 8, st));
     LaunchCfg cfg;
-    int rc = server_make_cfg(sv->s, kmax, efmax, n, &cfg);
+    int sbits = 0;
+    int rc = server_make_cfg(sv->s, kmax, efmax, n, &cfg, &sbits);
     if (rc) return rc;
     BatchView bv{};
     bv.queries = sv->dq.as<float>();
@@ -193,11 +196,8 @@ int launch_group(gsx_server *sv, Group *g, int si) {
     bv.status = sv->dstatus.as<int32_t>();
     bv.counter = cnt;
     bv.overflow = cnt + 1;
-    const int sbits = sv->s->tuning.spill_bits > 0 ? sv->s->tuning.spill_bits
-                                                   : std::min(16, std::max(14, cfg.L.table_bits + 3));
-    DevBuf &sp = *sv->spill[si];
-    if ((rc = sp.ensure((size_t)cfg.blocks * cfg.warps_per_block * ((size_t)1 << sbits) * 4))) return rc;
-    bv.gtab = sp.as<int32_t>();
+    if ((rc = sv->spill[si]->ensure((size_t)cfg.max_blocks * cfg.warps_per_block, sbits, st, &bv.gtab, &bv.gtab_epoch)))
+        return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(sv->s->ix, bv, cfg, st));
     for (Request *r : g->reqs) {
@@ -320,7 +320,7 @@ int gsx_server_create(gsx_searcher *s, int32_t max_queries_in_flight, int32_t km
         return bad(fail(GSX_ERR_NOMEM, "pinned host allocation failed"));
     sv->streams.resize(streams, nullptr);
     sv->running.assign(streams, nullptr);
-    for (int i = 0; i < streams; ++i) sv->spill.emplace_back(new DevBuf);
+    for (int i = 0; i < streams; ++i) sv->spill.emplace_back(new SpillTables);
     for (auto &st : sv->streams) {
         cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
         if (e != cudaSuccess) return bad(cuda_fail(e, "cudaStreamCreate"));
@@ -397,6 +397,73 @@ int gsx_server_stats(gsx_server *sv, int64_t *completed_queries, int32_t *queued
         *running_groups = n;
     }
     return GSX_OK;
+}
+
+int gsx_server_drive_poisson(gsx_server *sv, const float *queries, int32_t nq_pool, int32_t n_requests,
+                             double request_rate, int32_t size_min, int32_t size_max, const int32_t *ks, int32_t nk,
+                             const int32_t *efs, int32_t nef, uint64_t seed, double *latency_ms, int32_t *sizes,
+                             double *wall_s) {
+    if (!sv || !queries || !ks || !efs || !latency_ms || nk <= 0 || nef <= 0 || n_requests <= 0 || request_rate <= 0 ||
+        size_min <= 0 || size_max < size_min || size_max > nq_pool || size_max > sv->capacity)
+        return fail(GSX_ERR_INVALID, "bad load-driver arguments");
+    const int d = sv->d;
+    std::mt19937_64 rng(seed);
+    std::exponential_distribution<double> gap(request_rate);
+    std::uniform_real_distribution<double> u01(0.0, 1.0);
+    std::vector<double> at(n_requests);
+    std::vector<int32_t> sz(n_requests), kk(n_requests), ee(n_requests), off(n_requests);
+    double t = 0.0;
+    int64_t pos = 0;
+    const double lmin = std::log((double)size_min), lmax = std::log((double)size_max + 1.0);
+    for (int i = 0; i < n_requests; ++i) {
+        t += gap(rng);
+        at[i] = t;
+        sz[i] = std::min(size_max, (int32_t)std::floor(std::exp(lmin + (lmax - lmin) * u01(rng))));
+        kk[i] = ks[rng() % (uint64_t)nk];
+        ee[i] = efs[rng() % (uint64_t)nef];
+        if (pos + sz[i] > nq_pool) pos = 0;
+        off[i] = (int32_t)pos;
+        pos += sz[i];
+    }
+    std::vector<uint64_t> tickets(n_requests, 0);
+    std::atomic<int> submitted{0};
+    std::atomic<int> err{GSX_OK};
+    const auto t0 = Clock::now();
+    std::thread producer([&] {
+        for (int i = 0; i < n_requests; ++i) {
+            const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(at[i]));
+            // sleep most of the gap, then spin (bounded by the due time) for sub-millisecond precision
+            if (due - Clock::now() > std::chrono::microseconds(200))
+                std::this_thread::sleep_until(due - std::chrono::microseconds(100));
+            while (Clock::now() < due) {
+            }
+            uint64_t tk = 0;
+            const int rc = gsx_server_submit(sv, queries + (size_t)off[i] * d, sz[i], kk[i], ee[i], &tk);
+            if (rc != GSX_OK) {
+                err.store(rc);
+                break;
+            }
+            tickets[i] = tk;
+            submitted.store(i + 1, std::memory_order_release);
+        }
+    });
+    int rc = GSX_OK;
+    for (int i = 0; i < n_requests && rc == GSX_OK; ++i) {
+        while (submitted.load(std::memory_order_acquire) <= i) {
+            if (err.load() != GSX_OK) break;
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
+        if (err.load() != GSX_OK) {
+            rc = err.load();
+            break;
+        }
+        rc = gsx_server_wait(sv, tickets[i], 120000, nullptr, nullptr, &latency_ms[i]);
+        if (sizes) sizes[i] = sz[i];
+    }
+    producer.join();
+    if (wall_s) *wall_s = std::chrono::duration<double>(Clock::now() - t0).count();
+    if (rc == GSX_OK && err.load() != GSX_OK) rc = err.load();
+    return rc;
 }
 
 void gsx_server_destroy(gsx_server *sv) {

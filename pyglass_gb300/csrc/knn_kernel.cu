@@ -1,0 +1,471 @@
+// Exact k-nearest-neighbour ground truth by brute force on the 5th-generation tensor cores.
+//
+// The recall checks of the search need the exact top-k of every query over the whole base set.
+// Scores s = q.x come from bf16 tensor-core products with fp32 accumulation: each value is split
+// into hi = bf16(v) and lo = bf16(v - hi), and s = qh.xh + qh.xl + ql.xh (three MMAs into one
+// accumulator; one MMA when every input is exactly representable in bf16, e.g. integer data in
+// 0..255, which makes the scores exact).  The approximate distances (L2: |x|^2 - 2s, IP: -s) select
+// 16 candidates per query per half of every 128-column tile stream; the candidates are then
+// rescored exactly in fp64 on the CUDA cores and the top k (k <= 16) kept by (distance, id).
+//
+// Kernel layout (one CTA per SM, persistent over (query tile, base chunk) units):
+//   warp 0      TMA producer: query tile (128 x 128 bf16) and base tiles (128 x 128 bf16), 128-byte
+//               swizzled, two stages
+//   warp 1      TMEM allocation (256 columns = two 128x128 fp32 accumulators) and the MMA issuer
+//               (one elected thread, tcgen05.mma kind::f16, M=128 N=128 K=16)
+//   warps 4-11  epilogue: tcgen05.ld of the accumulator (warp w reads TMEM lanes 32*(w%4).., half
+//               (w-4)/4 of the columns), distance, per-query candidate list in shared memory
+// Every mbarrier wait is bounded; on timeout the CTA records an error and leaves after its copies
+// have drained, freeing its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gsx_host.h"
+
+namespace gsx {
+
+namespace {
+
+constexpr int kTM = 128;          // queries per tile (MMA M)
+constexpr int kTN = 128;          // base rows per tile (MMA N)
+constexpr int kKB = 64;           // bf16 elements per 128-byte swizzled K block
+constexpr int kCand = 16;         // candidates kept per query per epilogue half per unit
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 32 * (4 + kEpiWarps);
+constexpr uint32_t kTmemCols = 2 * kTN;  // two accumulators
+
+struct KnnParams {
+    int nq, N, dp;                // dp = padded dimension (multiple of 64)
+    int n_mt, n_chunks, tiles_per_chunk, n_tiles;
+    int passes;                   // 1 (exact bf16 inputs) or 3 (hi/lo split)
+    int ip;                       // 1 = inner product
+    const float *xnorm;           // N, |x|^2 (L2)
+    int32_t *cand;                // nq x n_chunks x 2 x kCand ids (-1 = none)
+    float *cand_d;                // matching approximate distances
+    unsigned *error;              // set on a timed-out wait
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// Waits for the phase of parity `par` to complete; false after ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t par) {
+    const uint32_t a = smem_u32(b);
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(a), "r"(par)
+            : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > 4000000000ll) return false;
+        __nanosleep(32);
+    }
+}
+
+__device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte swizzled layout: rows of
+// 128 bytes, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // descriptor version
+    d |= (uint64_t)2 << 61;             // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor: kind::f16, bf16 x bf16 -> fp32, both K-major, M x N.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct __align__(1024) KnnSmem {
+    // per pass p: query block [p][kb] and base block [stage][p][kb]; 1024-byte aligned blocks
+    __nv_bfloat16 q[2][2][kTM * kKB];          // [hi, lo][K block]          (2 x 2 x 16 KB)
+    __nv_bfloat16 x[2][2][2][kTN * kKB];       // [stage][hi, lo][K block]   (2 x 2 x 2 x 16 KB)
+};
+
+// dynamic shared memory carve-up (bytes): operands, then candidate lists, then barriers
+constexpr size_t kOpBytes = sizeof(KnnSmem);
+constexpr size_t kCandBytes = (size_t)kCand * kEpiWarps * 32 * 8;
+constexpr size_t kSmemBytes = kOpBytes + kCandBytes + 256 + 1024;
+
+__global__ void __launch_bounds__(kThreads, 1)
+knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__ CUtensorMap tq_lo,
+              const __grid_constant__ CUtensorMap tx_hi, const __grid_constant__ CUtensorMap tx_lo, KnnParams P) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    KnnSmem &S = *reinterpret_cast<KnnSmem *>(base);
+    float *cd = reinterpret_cast<float *>(base + kOpBytes);
+    int32_t *ci = reinterpret_cast<int32_t *>(base + kOpBytes + kCandBytes / 2);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + kOpBytes + kCandBytes);
+    uint64_t *full = bars, *empty = bars + 2, *tfull = bars + 4, *tempty = bars + 6, *qfull = bars + 8,
+             *qempty = bars + 9;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 12);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int kblocks = P.dp / kKB;  // 2 for d <= 128
+    const uint32_t qbytes = (uint32_t)(P.passes == 1 ? 1 : 2) * kblocks * kTM * kKB * 2;
+    const uint32_t xbytes = (uint32_t)(P.passes == 1 ? 1 : 2) * kblocks * kTN * kKB * 2;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+            mbar_init(&tfull[i], 1);
+            mbar_init(&tempty[i], kEpiWarps);
+        }
+        mbar_init(qfull, 1);
+        mbar_init(qempty, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int units = P.n_mt * P.n_chunks;
+    bool ok = true;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t it = 0, ut = 0;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x, ++ut) {
+                const int mt = u % P.n_mt, nc = u / P.n_mt;
+                if (!mbar_wait(qempty, (ut & 1) ^ 1)) { ok = false; break; }
+                mbar_expect_tx(qfull, qbytes);
+                for (int kb = 0; kb < kblocks; ++kb) {
+                    tma_2d(S.q[0][kb], &tq_hi, qfull, kb * kKB, mt * kTM);
+                    if (P.passes == 3) tma_2d(S.q[1][kb], &tq_lo, qfull, kb * kKB, mt * kTM);
+                }
+                const int t0 = nc * P.tiles_per_chunk, t1 = min(P.n_tiles, t0 + P.tiles_per_chunk);
+                for (int t = t0; t < t1; ++t, ++it) {
+                    const int st = it & 1;
+                    if (!mbar_wait(&empty[st], ((it >> 1) & 1) ^ 1)) { ok = false; break; }
+                    mbar_expect_tx(&full[st], xbytes);
+                    for (int kb = 0; kb < kblocks; ++kb) {
+                        tma_2d(S.x[st][0][kb], &tx_hi, &full[st], kb * kKB, t * kTN);
+                        if (P.passes == 3) tma_2d(S.x[st][1][kb], &tx_lo, &full[st], kb * kKB, t * kTN);
+                    }
+                }
+            }
+            if (!ok) atomicExch(P.error, 1u);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            uint32_t it = 0, ut = 0;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x, ++ut) {
+                const int nc = u / P.n_mt;
+                if (!mbar_wait(qfull, ut & 1)) { ok = false; break; }
+                const int t0 = nc * P.tiles_per_chunk, t1 = min(P.n_tiles, t0 + P.tiles_per_chunk);
+                for (int t = t0; t < t1; ++t, ++it) {
+                    const int st = it & 1, ab = it & 1;
+                    if (!mbar_wait(&full[st], (it >> 1) & 1)) { ok = false; break; }
+                    if (!mbar_wait(&tempty[ab], ((it >> 1) & 1) ^ 1)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d = tmem + (uint32_t)(ab * kTN);
+                    uint32_t acc = 0;
+                    // (hi, hi), then (hi, lo) and (lo, hi) for the split
+                    for (int pass = 0; pass < P.passes; ++pass) {
+                        const int qa = pass == 2 ? 1 : 0, xb = pass == 1 ? 1 : 0;
+                        for (int kb = 0; kb < kblocks; ++kb) {
+                            const uint32_t qa_addr = smem_u32(S.q[qa][kb]);
+                            const uint32_t xb_addr = smem_u32(S.x[st][xb][kb]);
+#pragma unroll
+                            for (int ks = 0; ks < kKB / 16; ++ks) {
+                                mma_bf16(d, sw128_desc(qa_addr + 32 * ks), sw128_desc(xb_addr + 32 * ks), acc);
+                                acc = 1;
+                            }
+                        }
+                    }
+                    mma_commit(&empty[st]);
+                    mma_commit(&tfull[ab]);
+                }
+                mma_commit(qempty);
+            }
+            if (!ok) atomicExch(P.error, 1u);
+        }
+    } else if (warp >= 4) {
+        const int ew = warp - 4;             // 0..7
+        const int quarter = warp & 3;        // TMEM lanes 32*quarter .. +31
+        const int half = ew >> 2;            // columns half*kTN/2 .. +kTN/2-1
+        const int slot = ew * 32 + lane;     // this thread's candidate list
+        const int row = quarter * 32 + lane; // query row within the tile
+        uint32_t it = 0;
+        for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+            const int mt = u % P.n_mt, nc = u / P.n_mt;
+            for (int c = 0; c < kCand; ++c) {
+                cd[c * kEpiWarps * 32 + slot] = __int_as_float(0x7f800000);
+                ci[c * kEpiWarps * 32 + slot] = -1;
+            }
+            float thr = __int_as_float(0x7f800000);
+            const int t0 = nc * P.tiles_per_chunk, t1 = min(P.n_tiles, t0 + P.tiles_per_chunk);
+            for (int t = t0; t < t1; ++t, ++it) {
+                const int ab = it & 1;
+                if (!mbar_wait(&tfull[ab], (it >> 1) & 1)) { ok = false; break; }
+                fence_after();
+                for (int c = 0; c < kTN / 64; ++c) {
+                    float v[32];
+                    const uint32_t col0 = (uint32_t)(ab * kTN + half * (kTN / 2) + c * 32);
+                    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + col0, v);
+                    const int n0 = t * kTN + half * (kTN / 2) + c * 32;
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int n = n0 + j;
+                        const float dist = n >= P.N ? __int_as_float(0x7f800000)
+                                           : (P.ip ? -v[j] : __ldg(P.xnorm + n) - 2.0f * v[j]);
+                        if (dist < thr) {
+                            // insert into the ascending list, dropping its last entry
+                            int pos = kCand - 1;
+                            while (pos > 0 && cd[(pos - 1) * kEpiWarps * 32 + slot] > dist) {
+                                cd[pos * kEpiWarps * 32 + slot] = cd[(pos - 1) * kEpiWarps * 32 + slot];
+                                ci[pos * kEpiWarps * 32 + slot] = ci[(pos - 1) * kEpiWarps * 32 + slot];
+                                --pos;
+                            }
+                            cd[pos * kEpiWarps * 32 + slot] = dist;
+                            ci[pos * kEpiWarps * 32 + slot] = n;
+                            thr = cd[(kCand - 1) * kEpiWarps * 32 + slot];
+                        }
+                    }
+                }
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&tempty[ab]);
+            }
+            const int qi = mt * kTM + row;
+            if (qi < P.nq) {
+                const size_t o = (((size_t)qi * P.n_chunks + nc) * 2 + half) * kCand;
+                for (int c = 0; c < kCand; ++c) {
+                    P.cand[o + c] = ci[c * kEpiWarps * 32 + slot];
+                    P.cand_d[o + c] = cd[c * kEpiWarps * 32 + slot];
+                }
+            }
+        }
+        if (!ok && lane == 0) atomicExch(P.error, 1u);
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+    }
+}
+
+// hi/lo bf16 split of fp32 rows, padded to dp columns; counts values whose lo part is nonzero.
+__global__ void split_bf16(const float *__restrict__ x, int64_t n, int d, int dp, __nv_bfloat16 *__restrict__ hi,
+                           __nv_bfloat16 *__restrict__ lo, unsigned *inexact) {
+    unsigned cnt = 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n * dp; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / dp;
+        const int j = (int)(t - r * dp);
+        const float v = j < d ? x[r * d + j] : 0.0f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const float rest = v - __bfloat162float(h);
+        hi[t] = h;
+        lo[t] = __float2bfloat16_rn(rest);
+        cnt += rest != 0.0f;
+    }
+    if (cnt) atomicAdd(inexact, cnt);
+}
+
+__global__ void row_norms(const float *__restrict__ x, int64_t n, int d, float *__restrict__ out) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0;
+        for (int j = 0; j < d; ++j) s += (double)x[r * d + j] * x[r * d + j];
+        out[r] = (float)s;
+    }
+}
+
+// One warp per query: exact fp64 distances of the candidates, top k by (distance, id).
+__global__ void rescore(const float *__restrict__ base, const float *__restrict__ queries, int nq, int d, int ncand,
+                        const int32_t *__restrict__ cand, int ip, int k, int32_t *__restrict__ out_ids,
+                        float *__restrict__ out_dis) {
+    extern __shared__ unsigned char sm[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int qi = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (qi >= nq) return;
+    double *dd = reinterpret_cast<double *>(sm) + (size_t)wib * ncand;
+    int32_t *id = reinterpret_cast<int32_t *>(reinterpret_cast<double *>(sm) + (size_t)(blockDim.x >> 5) * ncand) +
+                  (size_t)wib * ncand;
+    const float *q = queries + (size_t)qi * d;
+    for (int c = lane; c < ncand; c += 32) {
+        const int32_t n = cand[(size_t)qi * ncand + c];
+        double s = 0;
+        if (n >= 0) {
+            const float *x = base + (size_t)n * d;
+            for (int j = 0; j < d; ++j) {
+                const double a = q[j], b = x[j];
+                s += ip ? a * b : (a - b) * (a - b);
+            }
+            s = ip ? -s : s;
+        }
+        dd[c] = n >= 0 ? s : 1e300;
+        id[c] = n;
+    }
+    __syncwarp();
+    for (int c = lane; c < ncand; c += 32) {
+        const double dc = dd[c];
+        const int32_t ic = id[c];
+        if (ic < 0) continue;
+        int rank = 0;
+        for (int o = 0; o < ncand; ++o) {
+            const double x = dd[o];
+            const int32_t io = id[o];
+            rank += io >= 0 && (x < dc || (x == dc && io < ic));
+        }
+        if (rank < k) {
+            out_ids[(size_t)qi * k + rank] = ic;
+            out_dis[(size_t)qi * k + rank] = (float)dc;
+        }
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encode_map(CUtensorMap *m, void *ptr, int64_t rows, int dp, int box_rows) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+            return fail(GSX_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+        fn = (EncodeTiledFn)p;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)dp, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)dp * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kKB, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(GSX_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return GSX_OK;
+}
+
+}  // namespace
+
+}  // namespace gsx
+
+using namespace gsx;
+
+extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k,
+                             int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream) {
+    if (!d_base || !d_queries || !d_ids || !d_dis || N <= 0 || nq <= 0 || d <= 0)
+        return fail(GSX_ERR_INVALID, "bad arguments");
+    if (k <= 0 || k > kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", kCand);
+    if (d > 128) return fail(GSX_ERR_UNSUPPORTED, "exact kNN supports d <= 128");
+    if (N > (int64_t)INT32_MAX) return fail(GSX_ERR_INVALID, "N too large");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int dp = 128;  // two 64-element K blocks
+    DevBuf xh, xl, qh, ql, xn, cand, cand_d, cnt;
+    int rc;
+    if ((rc = xh.ensure((size_t)N * dp * 2)) || (rc = xl.ensure((size_t)N * dp * 2)) ||
+        (rc = qh.ensure((size_t)nq * dp * 2)) || (rc = ql.ensure((size_t)nq * dp * 2)) || (rc = xn.ensure((size_t)N * 4)) ||
+        (rc = cnt.ensure(16)))
+        return rc;
+    GSX_CUDA(cudaMemsetAsync(cnt.p, 0, 16, st));
+    split_bf16<<<4096, 256, 0, st>>>(d_base, N, d, dp, xh.as<__nv_bfloat16>(), xl.as<__nv_bfloat16>(), cnt.as<unsigned>());
+    split_bf16<<<1024, 256, 0, st>>>(d_queries, nq, d, dp, qh.as<__nv_bfloat16>(), ql.as<__nv_bfloat16>(),
+                                     cnt.as<unsigned>());
+    row_norms<<<1024, 256, 0, st>>>(d_base, N, d, xn.as<float>());
+    GSX_CUDA(cudaGetLastError());
+    unsigned inexact = 0;
+    GSX_CUDA(cudaMemcpyAsync(&inexact, cnt.p, 4, cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaStreamSynchronize(st));
+    if (exact_inputs) *exact_inputs = inexact == 0;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    KnnParams P{};
+    P.nq = nq;
+    P.N = (int)N;
+    P.dp = dp;
+    P.n_mt = (nq + kTM - 1) / kTM;
+    P.n_tiles = (int)((N + kTN - 1) / kTN);
+    // chunks so that units cover about four waves of the SMs
+    int chunks = std::max(1, (4 * nsm + P.n_mt - 1) / P.n_mt);
+    chunks = std::min(std::min(chunks, P.n_tiles), 16);  // at most 512 candidates per query
+    P.tiles_per_chunk = (P.n_tiles + chunks - 1) / chunks;
+    P.n_chunks = (P.n_tiles + P.tiles_per_chunk - 1) / P.tiles_per_chunk;
+    P.passes = inexact ? 3 : 1;
+    P.ip = ip ? 1 : 0;
+    P.xnorm = xn.as<float>();
+    const size_t ncand = (size_t)P.n_chunks * 2 * kCand;
+    if ((rc = cand.ensure((size_t)nq * ncand * 4)) || (rc = cand_d.ensure((size_t)nq * ncand * 4))) return rc;
+    P.cand = cand.as<int32_t>();
+    P.cand_d = cand_d.as<float>();
+    P.error = cnt.as<unsigned>() + 1;
+    CUtensorMap mqh, mql, mxh, mxl;
+    if ((rc = encode_map(&mqh, qh.p, nq, dp, kTM)) || (rc = encode_map(&mql, ql.p, nq, dp, kTM)) ||
+        (rc = encode_map(&mxh, xh.p, N, dp, kTN)) || (rc = encode_map(&mxl, xl.p, N, dp, kTN)))
+        return rc;
+    GSX_CUDA(cudaFuncSetAttribute(knn_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+    const int units = P.n_mt * P.n_chunks;
+    knn_tc_kernel<<<std::min(units, nsm), kThreads, kSmemBytes, st>>>(mqh, mql, mxh, mxl, P);
+    GSX_CUDA(cudaGetLastError());
+    const int wpb = 4;
+    const size_t rs_smem = (size_t)wpb * ncand * 12;
+    if (rs_smem > 227 * 1024) return fail(GSX_ERR_UNSUPPORTED, "too many candidate lists");
+    GSX_CUDA(cudaFuncSetAttribute(rescore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem));
+    rescore<<<(nq + wpb - 1) / wpb, wpb * 32, rs_smem, st>>>(d_base, d_queries, nq, d, (int)ncand, P.cand, P.ip, k,
+                                                             d_ids, d_dis);
+    GSX_CUDA(cudaGetLastError());
+    unsigned err = 0;
+    GSX_CUDA(cudaMemcpyAsync(&err, cnt.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaStreamSynchronize(st));
+    if (err) return fail(GSX_ERR_TIMEOUT, "tensor-core kNN kernel gave up waiting on a pipeline barrier");
+    return GSX_OK;
+}

@@ -312,6 +312,27 @@ struct Server {
         check(gsx_server_capacity(sv, &c));
         return c;
     }
+    // Open-loop Poisson load; returns (latency_ms[n], sizes[n], wall_s).
+    py::tuple drive_poisson(py::object queries, int n_requests, double request_rate, int size_min, int size_max,
+                            py::object ks, py::object efs, uint64_t seed) {
+        f32arr q(queries);
+        i32arr k(ks), e(efs);
+        size_t nq, features;
+        shape_of(q.request(), &nq, &features);
+        if ((int32_t)features != dim) throw std::runtime_error("glass-gb300: query dimension mismatch");
+        py::array_t<double> lat((py::ssize_t)n_requests);
+        py::array_t<int32_t> sz((py::ssize_t)n_requests);
+        double wall = 0;
+        int rc;
+        {
+            py::gil_scoped_release l;
+            rc = gsx_server_drive_poisson(sv, q.data(), (int32_t)nq, n_requests, request_rate, size_min, size_max,
+                                          k.data(), (int32_t)k.size(), e.data(), (int32_t)e.size(), seed,
+                                          lat.mutable_data(), sz.mutable_data(), &wall);
+        }
+        check(rc);
+        return py::make_tuple(lat, sz, wall);
+    }
     py::tuple stats() {
         int64_t done = 0;
         int32_t q = 0, r = 0;
@@ -328,6 +349,24 @@ PYBIND11_MODULE(_glass, m) {
     m.def("set_num_threads", [](int) {}, py::arg("num_threads"));
     m.def("version", []() { return std::string(gsx_version()); });
     m.def("device_count", []() { return gsx_device_count(); });
+    // Exact kNN ground truth on device buffers (integer pointers, e.g. torch data_ptr()); returns
+    // True when the single exact bf16 pass was used.
+    m.def(
+        "knn_exact",
+        [](uintptr_t base, int64_t N, int d, uintptr_t queries, int nq, int k, bool ip, uintptr_t ids, uintptr_t dis,
+           uintptr_t stream) {
+            int32_t exact = 0;
+            int rc;
+            {
+                py::gil_scoped_release l;
+                rc = gsx_knn_exact((const float *)base, N, d, (const float *)queries, nq, k, ip ? 1 : 0, (int32_t *)ids,
+                                   (float *)dis, &exact, (void *)stream);
+            }
+            check(rc);
+            return exact != 0;
+        },
+        py::arg("base"), py::arg("N"), py::arg("d"), py::arg("queries"), py::arg("nq"), py::arg("k"),
+        py::arg("ip") = false, py::arg("ids"), py::arg("dis"), py::arg("stream") = 0);
 
     py::class_<Graph>(m, "Graph")
         .def(py::init<>())
@@ -367,6 +406,9 @@ PYBIND11_MODULE(_glass, m) {
         .def("submit", &Server::submit, py::arg("query"), py::arg("k"), py::arg("ef"))
         .def("wait", &Server::wait, py::arg("ticket"), py::arg("nq"), py::arg("k"), py::arg("timeout_ms") = 60000)
         .def("capacity", &Server::capacity)
+        .def("drive_poisson", &Server::drive_poisson, py::arg("queries"), py::arg("n_requests"),
+             py::arg("request_rate"), py::arg("size_min"), py::arg("size_max"), py::arg("ks"), py::arg("efs"),
+             py::arg("seed") = 1)
         .def("stats", &Server::stats)
         .def("close", &Server::close);
 }

@@ -35,17 +35,41 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Visited set: open addressing with linear probing over 2^bits int32 slots (-1 = empty).
+// Visited set, open addressing with linear probing.  Two storages share the probe sequence:
+//  * the shared-memory table: 2^bits int32 slots, -1 = empty, cleared for every query;
+//  * the warp's global spill table: 2^bits uint64 slots holding (epoch << 32 | id), where a slot
+//    is empty unless its epoch is the query's own, so it is never cleared (epochs only grow).
 // Returns true if v was absent (and is now present).  Probing is bounded by the table size; the
 // caller keeps the load under 3/4 so a free slot always exists.
-__device__ __forceinline__ bool visit(int32_t *tab, int bits, int32_t v) {
+__device__ __forceinline__ uint32_t slot_of(int32_t v, int bits) { return ((uint32_t)v * 0x9E3779B1u) >> (32 - bits); }
+
+__device__ __forceinline__ bool visit_shared(int32_t *tab, int bits, int32_t v) {
     const uint32_t mask = (1u << bits) - 1u;
-    uint32_t h = ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
+    uint32_t h = slot_of(v, bits);
     for (uint32_t p = 0; p <= mask; ++p) {
         int32_t old = atomicCAS(tab + h, -1, v);
         if (old == -1) return true;
         if (old == v) return false;
         h = (h + 1u) & mask;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool visit_global(unsigned long long *tab, int bits, uint32_t epoch, int32_t v) {
+    const uint32_t mask = (1u << bits) - 1u;
+    const unsigned long long mine = ((unsigned long long)epoch << 32) | (uint32_t)v;
+    uint32_t h = slot_of(v, bits);
+    for (uint32_t p = 0; p <= mask;) {
+        const unsigned long long cur = *((volatile unsigned long long *)(tab + h));
+        if ((uint32_t)(cur >> 32) == epoch) {
+            if ((uint32_t)cur == (uint32_t)v) return false;
+            h = (h + 1u) & mask;
+            ++p;
+            continue;
+        }
+        const unsigned long long old = atomicCAS(tab + h, cur, mine);
+        if (old == cur) return true;
+        // another lane of this warp filled the slot first: look at it again
     }
     return false;
 }
@@ -80,29 +104,60 @@ struct WarpState {
     int32_t *acc_id;
     float *fq;
     uint32_t *qc;
-    int32_t *tab;
+    int32_t *tab;                // shared-memory table (null when the query runs on the spill table)
     int tbits;
-    int32_t *spill;  // this warp's global-memory table, used once the shared one is full
+    unsigned long long *spill;   // this warp's global table (epoch-tagged), or null
+    uint32_t *spill_epoch;       // its epoch counter
     int sbits;
-    int32_t *tab0;   // the table every query starts with
-    int tbits0;
+    uint32_t epoch;              // epoch of the current query in the spill table (0 = not used)
+    bool shared_first;           // queries start in the shared-memory table
 };
 
-// Moves the visited set from the shared-memory table into the warp's global table (cleared
-// first) and continues there: the set is unchanged, only its storage grows.
+__device__ __forceinline__ bool visit(WarpState &w, int32_t v) {
+    return w.epoch ? visit_global(w.spill, w.sbits, w.epoch, v) : visit_shared(w.tab, w.tbits, v);
+}
+
+// Starts a fresh epoch of the warp's spill table for the current query.
+__device__ __forceinline__ void spill_begin(WarpState &w, int lane) {
+    uint32_t e = 0;
+    if (lane == 0) e = atomicAdd(w.spill_epoch, 1u) + 1u;
+    w.epoch = __shfl_sync(kFull, e, 0);
+}
+
+// Moves the visited set from the shared-memory table into the warp's global spill table under a
+// fresh epoch and continues there: the set is unchanged, only its storage grows.  Each lane
+// re-inserts its share of the slots; first probes are issued eight at a time so that their
+// latencies overlap.
 __device__ __forceinline__ void migrate_visited(WarpState &w, int lane) {
-    const int gsize = 1 << w.sbits;
-    for (int j = lane * 4; j < gsize; j += 128) *reinterpret_cast<int4 *>(w.spill + j) = make_int4(-1, -1, -1, -1);
-    __syncwarp();
-    __threadfence_block();
+    spill_begin(w, lane);
     const int tsize = 1 << w.tbits;
-    for (int j = lane; j < tsize; j += 32) {
-        const int32_t v = w.tab[j];
-        if (v != -1) visit(w.spill, w.sbits, v);
+    const uint32_t mask = (1u << w.sbits) - 1u;
+    for (int j0 = lane; j0 < tsize; j0 += 32 * 8) {
+        int32_t v[8];
+        unsigned long long old[8];
+        uint32_t h[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int j = j0 + 32 * t;
+            v[t] = j < tsize ? w.tab[j] : -1;
+            h[t] = v[t] != -1 ? slot_of(v[t], w.sbits) : 0u;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            old[t] = 0;
+            if (v[t] != -1) {
+                const unsigned long long cur = *((volatile unsigned long long *)(w.spill + h[t]));
+                old[t] = (uint32_t)(cur >> 32) == w.epoch ? cur : atomicCAS(w.spill + h[t], cur, ((unsigned long long)w.epoch << 32) | (uint32_t)v[t]);
+                // the slot was ours to take when the CAS saw the value read
+                if ((uint32_t)(cur >> 32) != w.epoch && old[t] == cur) v[t] = -1;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (v[t] != -1) visit_global(w.spill, w.sbits, w.epoch, v[t]);
+        (void)mask;
     }
     __syncwarp();
-    w.tab = w.spill;
-    w.tbits = w.sbits;
 }
 
 // Merges candidates cand_{id,key}[0..m) (in insertion order, m <= 64) into the pool
@@ -118,23 +173,47 @@ __device__ __forceinline__ void migrate_visited(WarpState &w, int lane) {
 // other slot p takes the pool entry p - (candidates placed below p).  A chunk only reads entries
 // at or below its own slots, so no entry is overwritten before it is read.
 __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, int m, int lane) {
+    // survivors: with a full pool a candidate whose key is not below the last entry can never
+    // enter, and its larger key does not change the rank of one that does
+    const unsigned ltm = (1u << lane) - 1u;
+    const uint32_t last = S == cap ? w.pkey[S - 1] : 0xffffffffu;
+    const bool v0 = lane < m, v1 = lane + 32 < m;
+    const uint32_t k0 = v0 ? w.cand_key[lane] : 0u, k1 = v1 ? w.cand_key[lane + 32] : 0u;
+    const int32_t i0 = v0 ? w.cand_id[lane] : 0, i1 = v1 ? w.cand_id[lane + 32] : 0;
+    const bool s0 = v0 && (S < cap || k0 < last), s1 = v1 && (S < cap || k1 < last);
+    const unsigned b0 = __ballot_sync(kFull, s0), b1 = __ballot_sync(kFull, s1);
+    const int ns = __popc(b0) + __popc(b1);
+    if (ns == 0) {
+        S = (S + m) < cap ? (S + m) : cap;
+        return;
+    }
+    // compact the survivors in arrival order
+    __syncwarp();
+    if (s0) {
+        const int t = __popc(b0 & ltm);
+        w.cand_key[t] = k0;
+        w.cand_id[t] = i0;
+    }
+    if (s1) {
+        const int t = __popc(b0) + __popc(b1 & ltm);
+        w.cand_key[t] = k1;
+        w.cand_id[t] = i1;
+    }
+    __syncwarp();
     int nacc = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int j = lane + 32 * h;
-        const bool valid = j < m;
-        uint32_t kj = valid ? w.cand_key[j] : 0u;
+        const bool valid = j < ns;
+        const uint32_t kj = valid ? w.cand_key[j] : 0u;
         int acc = 0, ub = 0, rank = 0;
         if (valid) {
-            bool reject = (S == cap) && kj >= w.pkey[S - 1];
-            if (!reject) {
-                for (int i = 0; i < m; ++i) {
-                    uint32_t ki = w.cand_key[i];
-                    rank += (ki < kj) || (ki == kj && i < j);
-                }
-                ub = upper_bound_u32(w.pkey, S, kj);
-                acc = (ub + rank) < cap;
+            for (int i = 0; i < ns; ++i) {
+                const uint32_t ki = w.cand_key[i];
+                rank += (ki < kj) || (ki == kj && i < j);
             }
+            ub = upper_bound_u32(w.pkey, S, kj);
+            acc = (ub + rank) < cap;
         }
         if (acc) {
             w.acc_ub[rank] = ub;
@@ -142,7 +221,7 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
             w.acc_id[rank] = w.cand_id[j];
         }
         nacc += __popc(__ballot_sync(kFull, acc));
-        if (m <= 32) break;
+        if (ns <= 32) break;
     }
     __syncwarp();
     if (nacc == 0) return;
@@ -154,7 +233,6 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     const int p1 = ub1 == kNone ? kNone : ub1 + lane + 32;
     const int lo = __shfl_sync(kFull, p0, 0);  // slot of the rank-0 candidate = acc_ub[0]
     const int newS = (S + m) < cap ? (S + m) : cap;
-    const unsigned ltm = (1u << lane) - 1u;
     const int nchunks = (newS - lo + 31) >> 5;
     for (int c = nchunks - 1; c >= 0; --c) {
         const int base = lo + 32 * c;
@@ -231,6 +309,37 @@ __device__ __forceinline__ void refine_dists(const IndexView &ix, const int32_t 
     __syncwarp();
 }
 
+// The node the next expansion will pop, known before the merge: the first unexpanded pool entry,
+// unless the best candidate that can enter has a strictly smaller key (equal keys go after the
+// pool entry).  Used only to start loading that node's adjacency row early; the pop checks it.
+__device__ __forceinline__ int predict_next(const WarpState &w, int S, int cap, int lb, int lim, int m, int lane) {
+    const int hi = S < lim ? S : lim;
+    const int f0 = first_unchecked(w.pid, lb, hi, lane);
+    const bool has_pool = f0 < hi;
+    const uint32_t kf = has_pool ? w.pkey[f0] : 0xffffffffu;
+    const uint32_t last = S == cap ? w.pkey[S - 1] : 0xffffffffu;
+    uint32_t bk = 0xffffffffu;
+    int bj = kMaxDegree;
+    for (int j = lane; j < m; j += 32) {
+        const uint32_t k = w.cand_key[j];
+        if ((S < cap || k < last) && (k < bk || (k == bk && j < bj))) {
+            bk = k;
+            bj = j;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t ok = __shfl_xor_sync(kFull, bk, o);
+        const int oj = __shfl_xor_sync(kFull, bj, o);
+        if (ok < bk || (ok == bk && oj < bj)) {
+            bk = ok;
+            bj = oj;
+        }
+    }
+    if (bj < kMaxDegree && (!has_pool || bk < kf)) return w.cand_id[bj];
+    return has_pool ? (w.pid[f0] & kIdMask) : -1;
+}
+
 // Encodes the query held in w.fq into w.qc (SQ kinds); returns the sum of squared codes.
 template <int KIND, int METRIC>
 __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState &w, int lane) {
@@ -278,13 +387,19 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
     __syncwarp();
     const int32_t qsq = prepare_query<KIND, METRIC>(ix, w, lane);
 
-    // visited table reset (back to the shared-memory table if the last query spilled)
-    w.tab = w.tab0;
-    w.tbits = w.tbits0;
-    const int tsize = 1 << w.tbits;
-    for (int j = lane * 4; j < tsize; j += 128) *reinterpret_cast<int4 *>(w.tab + j) = make_int4(-1, -1, -1, -1);
-    __syncwarp();
-    int tlimit = (tsize >> 2) * 3;
+    // visited set: a cleared shared-memory table, or (when the launch has none) a fresh epoch of
+    // the spill table
+    int tlimit;
+    if (w.shared_first) {
+        w.epoch = 0;
+        const int tsize = 1 << w.tbits;
+        for (int j = lane * 4; j < tsize; j += 128) *reinterpret_cast<int4 *>(w.tab + j) = make_int4(-1, -1, -1, -1);
+        __syncwarp();
+        tlimit = (tsize >> 2) * 3;
+    } else {
+        spill_begin(w, lane);
+        tlimit = ((1 << w.sbits) >> 2) * 3;
+    }
 
     int S = 0, lb = 0, nvis = 0, cmps = 0, nexp = 0;
     bool overflow = false;
@@ -347,7 +462,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         __syncwarp();
         merge(w, S, cap, lb, 1, lane);
-        if (lane == 0) visit(w.tab, w.tbits, u);
+        if (lane == 0) visit(w, u);
         nvis += 1;
         __syncwarp();
     } else {
@@ -358,7 +473,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
             cmps += m;
             merge(w, S, cap, lb, m, lane);
-            for (int j = lane; j < m; j += 32) visit(w.tab, w.tbits, w.cand_id[j]);
+            for (int j = lane; j < m; j += 32) visit(w, w.cand_id[j]);
             nvis += m;
             __syncwarp();
             if (nvis > tlimit) { overflow = true; break; }
@@ -367,13 +482,15 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
 
     // ---- SearchImpl2 (graph_searcher.hpp:196-224) ----
     const int lim = ef_expand < cap ? ef_expand : cap;
+    int pred_u = -1;             // node whose row was loaded speculatively during the last merge
+    int32_t pv0 = -1, pv1 = -1;  // that row: entries lane and 32 + lane
     while (!overflow) {
         const int f = first_unchecked(w.pid, lb, S < lim ? S : lim, lane);
         if (f >= S || f >= lim) break;
         if (nvis + ix.K > tlimit) {
-            if (w.spill && w.tab != w.spill) {
+            if (w.spill && w.epoch == 0) {
                 migrate_visited(w, lane);
-                tlimit = ((1 << w.tbits) >> 2) * 3;
+                tlimit = ((1 << w.sbits) >> 2) * 3;
             }
             if (nvis + ix.K > tlimit) { overflow = true; break; }
         }
@@ -384,18 +501,22 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         lb = f + 1;
         ++nexp;
         // adjacency row, stop at the first -1; skip repeats within the row and visited ids
-        const int32_t *row = ix.adj + (size_t)u * (size_t)ix.K;
+        int32_t r0 = pv0, r1 = pv1;
+        if (u != pred_u) {
+            const int32_t *row = ix.adj + (size_t)u * (size_t)ix.K;
+            r0 = lane < ix.K ? __ldg(row + lane) : -1;
+            r1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
+        }
         int m = 0;
         for (int c0 = 0; c0 < ix.K; c0 += 32) {
-            const int i = c0 + lane;
-            const int v = i < ix.K ? __ldg(row + i) : -1;
+            const int v = c0 == 0 ? r0 : r1;
             const unsigned endm = __ballot_sync(kFull, v == -1);
             const int nvalid = endm ? __ffs(endm) - 1 : 32;
             const bool valid = lane < nvalid;
             const unsigned same = __match_any_sync(kFull, v);
             const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
             const bool first = valid && ((same & vmask & lanemask_lt()) == 0);
-            const bool fresh = first && visit(w.tab, w.tbits, v);
+            const bool fresh = first && visit(w, v);
             const unsigned nm = __ballot_sync(kFull, fresh);
             if (fresh) w.cand_id[m + __popc(nm & lanemask_lt())] = v;
             m += __popc(nm);
@@ -403,17 +524,32 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         __syncwarp();
         nvis += m;
-        if (m == 0) continue;
+        if (m == 0) {
+            pred_u = -1;
+            continue;
+        }
         compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
         cmps += m;
+        // start the next row's load now, so that it arrives while the merge runs
+        pred_u = predict_next(w, S, cap, lb, lim, m, lane);
+        if (pred_u >= 0) {
+            const int32_t *row = ix.adj + (size_t)pred_u * (size_t)ix.K;
+            pv0 = lane < ix.K ? __ldg(row + lane) : -1;
+            pv1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
+        }
         merge(w, S, cap, lb, m, lane);
-        if (L.prefetch) {
-            // LinearPool insert success -> graph.prefetch (graph_searcher.hpp:189-191): pull the
-            // adjacency rows of the first few pool entries towards L2
-            const int i = lb + lane;
-            if (lane < 4 && i < S && w.pid[i] >= 0) {
-                const int32_t *r = ix.adj + (size_t)(w.pid[i] & kIdMask) * (size_t)ix.K;
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(r));
+        if (L.prefetch && pred_u >= 0) {
+            // the predicted row has arrived during the merge: pull its neighbours' code rows
+            // towards L1 for the next expansion (a wrong prediction only wastes the prefetch;
+            // cf. the reference's computer.prefetch, graph_searcher.hpp:212-218)
+            const int lines = ix.csize > 128 ? 2 : 1;
+            if (pv0 >= 0) {
+                const uint8_t *c = ix.codes + (size_t)pv0 * (size_t)ix.csize;
+                for (int l = 0; l < lines; ++l) asm volatile("prefetch.global.L1 [%0];" ::"l"(c + 128 * l));
+            }
+            if (pv1 >= 0) {
+                const uint8_t *c = ix.codes + (size_t)pv1 * (size_t)ix.csize;
+                for (int l = 0; l < lines; ++l) asm volatile("prefetch.global.L1 [%0];" ::"l"(c + 128 * l));
             }
         }
     }
@@ -507,16 +643,12 @@ __global__ void __launch_bounds__(256) search_kernel(IndexView ix, BatchView bv,
     w.qc = reinterpret_cast<uint32_t *>(ws + L.qc);
     const size_t slot = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     w.spill = bv.gtab ? bv.gtab + (slot << bv.gtab_bits) : nullptr;
+    w.spill_epoch = bv.gtab ? bv.gtab_epoch + slot : nullptr;
     w.sbits = bv.gtab_bits;
-    if (L.table_bits > 0) {
-        w.tab0 = reinterpret_cast<int32_t *>(ws + L.table);
-        w.tbits0 = L.table_bits;
-    } else {
-        w.tab0 = w.spill;
-        w.tbits0 = bv.gtab_bits;
-    }
-    w.tab = w.tab0;
-    w.tbits = w.tbits0;
+    w.epoch = 0;
+    w.shared_first = L.table_bits > 0;
+    w.tab = reinterpret_cast<int32_t *>(ws + L.table);
+    w.tbits = L.table_bits;
     while (true) {
         unsigned t = 0;
         if (lane == 0) t = atomicAdd(bv.counter, 1u);

@@ -45,7 +45,12 @@ def low_rank(n: int, d: int = 960, rank: int = 32, noise: float = 0.05, seed: in
         m = min(_CHUNK, n - s)
         z = rng.standard_normal((m, rank), dtype=np.float32)
         e = rng.standard_normal((m, d), dtype=np.float32) * np.float32(noise)
-        out[s:s + m] = z @ w.T + e
+        # elementwise float64 products summed in a fixed order: a BLAS product would round
+        # differently on different hosts
+        acc = e.astype(np.float64)
+        for r in range(rank):
+            acc += z[:, r:r + 1].astype(np.float64) * w[:, r].astype(np.float64)
+        out[s:s + m] = acc
     return out
 
 
@@ -78,12 +83,32 @@ WORKLOADS = {
     "lowrank100k": dict(base=lambda: low_rank(100_000, 960, seed=3), queries=lambda: low_rank(1_000, 960, seed=3, stream=1),
                         index=("HNSW", 32, 200, "SQ8U"), metric="L2",
                         desc="100,000 x 960 low-rank (x = Wz + e, rank 32, noise 0.05), HNSW R=32 L=200, 1,000 queries"),
+    "lowrank1m": dict(base=lambda: low_rank(1_000_000, 960, seed=3), queries=lambda: low_rank(1_000, 960, seed=3, stream=1),
+                      index=("HNSW", 32, 200, "SQ8U"), metric="L2",
+                      desc="1,000,000 x 960 low-rank (x = Wz + e, rank 32, noise 0.05), HNSW R=32 L=200, 1,000 queries"),
+    "sphere2m": dict(base=lambda: normalized_mixture(2_000_000, 768, seed=4),
+                     queries=lambda: normalized_mixture(10_000, 768, seed=4, stream=1),
+                     index=("NSG", 48, 100, "SQ8U"), metric="IP",
+                     desc="2,000,000 x 768 unit vectors from 4,096 clusters (sigma 0.3), NSG R=48 L=100 (L2 build), "
+                          "10,000 queries, inner product"),
     "sphere200k": dict(base=lambda: normalized_mixture(200_000, 768, seed=4),
                        queries=lambda: normalized_mixture(2_000, 768, seed=4, stream=1),
                        index=("NSG", 48, 100, "SQ8U"), metric="IP",
                        desc="200,000 x 768 unit vectors from 4,096 clusters (sigma 0.3), NSG R=48 L=100 (L2 build), "
                             "2,000 queries, inner product"),
 }
+
+
+def graph_file(name: str, root: str) -> tuple[str, str] | None:
+    """(path, format) of a workload's graph under root/data: the glass file, else its compact
+    NSG-format twin; None when neither exists."""
+    import os
+
+    for ext, fmt in ((".glass", "glass"), (".nsg", "nsg")):
+        p = os.path.join(root, "data", name + ext)
+        if os.path.exists(p):
+            return p, fmt
+    return None
 
 
 def checksum(a: np.ndarray) -> str:

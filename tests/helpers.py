@@ -41,3 +41,15 @@ def knn_graph(x, K, rng, drop=0.3, dup=0.05):
 
 def recall(ids, gt, k):
     return float(np.mean([len(np.intersect1d(ids[i, :k], gt[i, :k])) for i in range(ids.shape[0])])) / k
+
+
+def oracle_graph(oracle, glass, path, fmt):
+    """The oracle reads glass files only: other formats are converted through the library's loader."""
+    if fmt == "glass":
+        return oracle.Graph(path)
+    import os
+    import tempfile
+
+    tmp = os.path.join(tempfile.mkdtemp(), "g.glass")
+    glass.Graph(path, fmt).save(tmp)
+    return oracle.Graph(tmp)

@@ -8,17 +8,18 @@ import numpy as np
 import pytest
 
 from pyglass_gb300 import datasets
+from tests.helpers import oracle_graph
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-GRAPH = os.path.join(ROOT, "data", "clusters1m.glass")
+FOUND = datasets.graph_file("clusters1m", ROOT)
 
 
 @pytest.fixture(scope="module")
 def workload():
-    if not os.path.exists(GRAPH):
+    if FOUND is None:
         pytest.skip("data/clusters1m.glass not present (built by oracle/build_graphs.py)")
-    meta = json.load(open(GRAPH.replace(".glass", ".json")))
+    meta = json.load(open(os.path.join(ROOT, "data", "clusters1m.json")))
     w = datasets.WORKLOADS["clusters1m"]
     base, q = w["base"](), w["queries"]()
     assert datasets.checksum(base) == meta["base_checksum"], "synthetic base differs from the one the graph was built on"
@@ -27,8 +28,8 @@ def workload():
 
 def test_clusters1m_sq4u_refine_matches_oracle(gpu, oracle, workload):
     base, q = workload
-    s = gpu.Searcher(gpu.Graph(GRAPH), base, "L2", "SQ4U", "FP32")
-    o = oracle.Searcher(oracle.Graph(GRAPH), base, "L2", "SQ4U", "FP32")
+    s = gpu.Searcher(gpu.Graph(*FOUND), base, "L2", "SQ4U", "FP32")
+    o = oracle.Searcher(oracle_graph(oracle, gpu, *FOUND), base, "L2", "SQ4U", "FP32")
     for ef in (16, 64):
         s.set_ef(ef)
         o.set_ef(ef)

@@ -73,3 +73,16 @@ def test_limits_and_timeouts(gpu, searcher):
     with pytest.raises(RuntimeError, match="unknown ticket"):
         srv.wait(987654, 1, 10, timeout_ms=10)
     srv.close()
+
+
+def test_poisson_driver(gpu, searcher):
+    srv = gpu.Server(searcher, capacity=512, kmax=40, efmax=96, streams=4)
+    q = np.concatenate([spec.queries(), spec.base()[:500]])
+    lat, sizes, wall = srv.drive_poisson(q, 300, 3000.0, 1, 64, [1, 10, 40], [8, 32, 96], seed=3)
+    assert lat.shape == (300,) and sizes.min() >= 1 and sizes.max() <= 64
+    assert np.all(lat > 0) and wall > 0
+    done, queued, running = srv.stats()
+    assert done == int(sizes.sum()) and queued == 0
+    with pytest.raises(RuntimeError, match="load-driver"):
+        srv.drive_poisson(q, 10, 100.0, 1, 1000, [10], [32])  # size_max above the admitted slots
+    srv.close()
