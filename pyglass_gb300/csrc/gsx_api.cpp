@@ -54,17 +54,16 @@ void DevBuf::release() {
     bytes = 0;
 }
 
-int SpillTables::ensure(size_t n, int b, cudaStream_t st, unsigned long long **tab, uint32_t **epoch) {
-    const size_t tbytes = n * ((size_t)1 << b) * 8;
+int SpillTables::ensure(size_t n, int b, cudaStream_t st, int32_t **tab) {
+    const size_t bytes = n * ((size_t)1 << b) * 8;  // table + slot list per warp
     if (!buf.p || n != slots || b != bits) {
-        int rc = buf.ensure(tbytes + n * 4);
+        int rc = buf.ensure(bytes);
         if (rc) return rc;
-        GSX_CUDA(cudaMemsetAsync(buf.p, 0, tbytes + n * 4, st));
+        GSX_CUDA(cudaMemsetAsync(buf.p, 0, bytes, st));
         slots = n;
         bits = b;
     }
-    *tab = buf.as<unsigned long long>();
-    *epoch = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(buf.p) + tbytes);
+    *tab = buf.as<int32_t>();
     return GSX_OK;
 }
 
@@ -166,8 +165,9 @@ int kin_of(const gsx_searcher *s, int k) {
 int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int table_bits_override, LaunchCfg *cfg) {
     const int cap = std::max(kin_of(s, kmax), efmax);
     if (cap > kMaxCap) return fail(GSX_ERR_UNSUPPORTED, "pool capacity %d (k, ef) exceeds %d", cap, kMaxCap);
-    int bits = table_bits_override > 0 ? table_bits_override
-               : (s->tuning.table_bits > 0 ? s->tuning.table_bits : default_table_bits(s, efmax));
+    // default: the visited set lives in the warp's global table (the shared memory it would take
+    // buys more resident warps instead)
+    int bits = table_bits_override > 0 ? table_bits_override : (s->tuning.table_bits > 0 ? s->tuning.table_bits : kGlobalOnly);
     int wpb = single ? 1 : (s->tuning.warps_per_block > 0 ? s->tuning.warps_per_block : 4);
     int lpr = s->tuning.lanes_per_row > 0 ? s->tuning.lanes_per_row
               : ((s->kind == K_E5M2 || s->kind == K_FP32) ? 4 : (s->ix.csize > 256 ? 4 : 1));
@@ -194,13 +194,15 @@ int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int tabl
     return GSX_OK;
 }
 
-// Global (spill) table size: room for the largest visit count seen on this searcher at a 3/4 load
-// (2^12..2^16 slots), else 4x the shared table.
+// Global (spill) table size.  Every probe past the first costs another L2 round trip, so the table
+// is kept sparse: about 8x the largest visit count seen on this searcher (12% load), 2^14..2^17
+// slots.
 int spill_bits_for(const gsx_searcher *s, const LaunchCfg &cfg) {
+    (void)cfg;
     if (s->tuning.spill_bits > 0) return s->tuning.spill_bits;
-    int bits = 12;
-    const int64_t want = s->visit_hint > 0 ? (int64_t)s->visit_hint * 4 / 3 + 2 * s->ix.K : (int64_t)1 << (cfg.L.table_bits + 2);
-    while ((1ll << bits) < want && bits < 16) ++bits;
+    int bits = 14;
+    const int64_t want = s->visit_hint > 0 ? (int64_t)s->visit_hint * 8 : 0;
+    while ((1ll << bits) < want && bits < 17) ++bits;
     return bits;
 }
 
@@ -239,7 +241,7 @@ int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int3
     // one spill table per resident warp of this launch shape, 4x the shared table (>= 2^13 slots)
     const int sbits = spill_bits_for(s, cfg);
     const size_t slots = (size_t)cfg.max_blocks * cfg.warps_per_block;
-    if ((rc = s->spill.ensure(slots, sbits, st, &bv.gtab, &bv.gtab_epoch))) return rc;
+    if ((rc = s->spill.ensure(slots, sbits, st, &bv.gtab))) return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     return GSX_OK;
@@ -267,12 +269,11 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     if (rc) return rc;
     cfg.L.table_bits = 0;
     cfg.warps_per_block = 4;
-    const int slots_max = 64;
+    const int slots_max = 16;
     cfg.blocks = std::max(1, std::min(((int)redo.size() + 3) / 4, slots_max / 4));
     const size_t slots = (size_t)cfg.blocks * cfg.warps_per_block;
-    unsigned long long *gt = nullptr;
-    uint32_t *ge = nullptr;
-    if ((rc = s->gtab.ensure(slots, gbits, st, &gt, &ge))) return rc;
+    int32_t *gt = nullptr;
+    if ((rc = s->gtab.ensure(slots, gbits, st, &gt))) return rc;
     if ((rc = upload(s->order, redo.data(), redo.size(), st))) return rc;
     if ((rc = s->status.ensure((size_t)nq * 4))) return rc;
     GSX_CUDA(cudaMemsetAsync(s->counters.p, 0, 8, st));
@@ -293,7 +294,6 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
     bv.gtab = gt;
-    bv.gtab_epoch = ge;
     bv.gtab_bits = gbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     GSX_CUDA(cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
@@ -676,6 +676,7 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
     if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
         return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
                     kMinTableBits);
+    if (t->prefetch < 0 || t->prefetch > 3) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 3]");
     if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
         return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
     s->tuning = *t;
@@ -705,13 +706,21 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
     std::vector<int> lprs = (s->kind == K_E5M2 || s->kind == K_FP32) ? std::vector<int>{1, 4} : std::vector<int>{1, 2, 4};
     gsx_tuning best = saved;
     float best_ms = 1e30f;
-    // shared tables from 2^8 slots up to the default size, and none at all (global table only)
-    std::vector<int> bit_choices{kGlobalOnly};
-    for (int b = 8; b <= std::max(8, base_bits); ++b) bit_choices.push_back(b);
-    for (int wpb : {1, 2, 4})
+    // visited sets in global tables only, or a small shared table in front; sparse global tables
+    std::vector<int> bit_choices{kGlobalOnly, 9};
+    (void)base_bits;
+    const int sb0 = s->tuning.spill_bits;
+    s->tuning.spill_bits = 0;
+    LaunchCfg probe;
+    int auto_sb = 14;
+    if (make_cfg(s, k, s->ef, nq, false, 0, &probe) == GSX_OK) auto_sb = spill_bits_for(s, probe);
+    s->tuning.spill_bits = sb0;
+    for (int wpb : {2, 4})
         for (int lpr : lprs)
-            for (int bits : bit_choices) {
-                gsx_tuning t{wpb, bits, lpr, saved.prefetch, saved.spill_bits};
+            for (int bits : bit_choices)
+            for (int pf : {0, 1})
+            for (int sb : {auto_sb, auto_sb + 1}) {
+                gsx_tuning t{wpb, bits, lpr, pf, sb};
                 s->tuning = t;
                 float ms_min = 1e30f;
                 bool ok = true;

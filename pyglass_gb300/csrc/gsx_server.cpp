@@ -96,7 +96,7 @@ struct Ranges {
 
 struct gsx_server {
     gsx_searcher *s = nullptr;
-    int capacity = 0, kcap = 0, efcap = 0, nstreams = 0, d = 0;
+    int capacity = 0, kcap = 0, efcap = 0, nstreams = 0, d = 0, max_group = 0;
     std::vector<cudaStream_t> streams;
     std::vector<Group *> running;  // per stream
     DevBuf dq, dids, ddis, dk, def, dstatus, dorder, dcnt;
@@ -174,6 +174,10 @@ int launch_group(gsx_server *sv, Group *g, int si) {
         GSX_CUDA(cudaMemcpyAsync(sv->dk.as<int32_t>() + o, sv->hk + o, (size_t)r->nq * 4, cudaMemcpyHostToDevice, st));
         GSX_CUDA(cudaMemcpyAsync(sv->def.as<int32_t>() + o, sv->hef + o, (size_t)r->nq * 4, cudaMemcpyHostToDevice, st));
     }
+    // longest searches first (largest ef, then k), so that the group's tail is short
+    std::stable_sort(order, order + n, [&](int32_t a, int32_t b) {
+        return sv->hef[a] != sv->hef[b] ? sv->hef[a] > sv->hef[b] : sv->hk[a] > sv->hk[b];
+    });
     int32_t *dorder = sv->dorder.as<int32_t>() + (size_t)si * sv->capacity;
     GSX_CUDA(cudaMemcpyAsync(dorder, order, (size_t)n * 4, cudaMemcpyHostToDevice, st));
     unsigned *cnt = sv->dcnt.as<unsigned>() + 2 * si;
@@ -196,8 +200,7 @@ int launch_group(gsx_server *sv, Group *g, int si) {
     bv.status = sv->dstatus.as<int32_t>();
     bv.counter = cnt;
     bv.overflow = cnt + 1;
-    if ((rc = sv->spill[si]->ensure((size_t)cfg.max_blocks * cfg.warps_per_block, sbits, st, &bv.gtab, &bv.gtab_epoch)))
-        return rc;
+    if ((rc = sv->spill[si]->ensure((size_t)cfg.max_blocks * cfg.warps_per_block, sbits, st, &bv.gtab))) return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(sv->s->ix, bv, cfg, st));
     for (Request *r : g->reqs) {
@@ -240,13 +243,18 @@ void dispatcher(gsx_server *sv) {
         if (si >= 0 && !sv->queue.empty()) {
             auto *g = new Group;
             g->wake = &sv->cv;
+            int gq = 0;
             while (!sv->queue.empty()) {
                 Request *r = sv->queue.front();
+                // groups stay small enough that slots cycle quickly: a group's slots free only when
+                // its slowest query is done
+                if (gq > 0 && gq + r->nq > sv->max_group) break;
                 const int s0 = sv->ranges.take(r->nq);
                 if (s0 < 0) break;  // wait for slots to free (FIFO: no overtaking)
                 r->slot0 = s0;
                 r->state = 1;
                 g->reqs.push_back(r);
+                gq += r->nq;
                 sv->queue.pop_front();
             }
             if (!g->reqs.empty()) {
@@ -304,6 +312,7 @@ int gsx_server_create(gsx_searcher *s, int32_t max_queries_in_flight, int32_t km
     size_t cap = (size_t)max_queries_in_flight;
     if (per_slot * cap > free_b / 2) cap = std::max<size_t>(1, free_b / 2 / per_slot);
     sv->capacity = (int)cap;
+    sv->max_group = std::max(256, sv->capacity / (2 * streams));
     auto bad = [&](int code) {
         gsx_server_destroy(sv);
         return code;

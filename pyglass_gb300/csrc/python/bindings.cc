@@ -397,12 +397,12 @@ PYBIND11_MODULE(_glass, m) {
         .def("calibration", &Searcher::calibration)
         .def("get_tuning", &Searcher::get_tuning)
         .def("set_tuning", &Searcher::set_tuning, py::arg("warps_per_block") = 0, py::arg("table_bits") = 0,
-             py::arg("lanes_per_row") = 0, py::arg("prefetch") = 1, py::arg("spill_bits") = 0)
+             py::arg("lanes_per_row") = 0, py::arg("prefetch") = 2, py::arg("spill_bits") = 0)
         .def("memory", &Searcher::memory);
 
     py::class_<Server>(m, "Server")
         .def(py::init<py::object, int, int, int, int>(), py::arg("searcher"), py::arg("capacity") = 16384,
-             py::arg("kmax") = 100, py::arg("efmax") = 256, py::arg("streams") = 4)
+             py::arg("kmax") = 100, py::arg("efmax") = 256, py::arg("streams") = 8)
         .def("submit", &Server::submit, py::arg("query"), py::arg("k"), py::arg("ef"))
         .def("wait", &Server::wait, py::arg("ticket"), py::arg("nq"), py::arg("k"), py::arg("timeout_ms") = 60000)
         .def("capacity", &Server::capacity)

@@ -37,17 +37,21 @@ def cluster_mixture(n: int, d: int = 128, n_clusters: int = 1024, sigma: float =
 
 
 def low_rank(n: int, d: int = 960, rank: int = 32, noise: float = 0.05, seed: int = 3, stream: int = 0) -> np.ndarray:
-    """x = W z + e with z ~ N(0, I_rank), W (d x rank) ~ N(0, 1/rank) shared per seed, e ~ N(0, noise^2)."""
+    """x = W z + e with z ~ N(0, I_rank), W (d x rank) ~ N(0, 1/rank) shared per seed, e zero-mean noise
+    of standard deviation `noise` (a scaled sum of four uniforms)."""
     w = np.random.default_rng([seed, 999]).normal(0.0, 1.0 / np.sqrt(rank), size=(d, rank)).astype(np.float32)
     rng = np.random.default_rng([seed, stream])
     out = np.empty((n, d), np.float32)
-    for s in range(0, n, _CHUNK):
-        m = min(_CHUNK, n - s)
+    step = 10_000
+    for s in range(0, n, step):
+        m = min(step, n - s)
         z = rng.standard_normal((m, rank), dtype=np.float32)
-        e = rng.standard_normal((m, d), dtype=np.float32) * np.float32(noise)
+        # noise: a sum of four uniforms, centred and scaled to sd `noise` (built from integer-derived
+        # doubles only, so every host produces the same bytes)
+        u = rng.random((4, m, d))
+        acc = (u[0] + u[1] + u[2] + u[3] - 2.0) * (np.sqrt(3.0) * noise)
         # elementwise float64 products summed in a fixed order: a BLAS product would round
         # differently on different hosts
-        acc = e.astype(np.float64)
         for r in range(rank):
             acc += z[:, r:r + 1].astype(np.float64) * w[:, r].astype(np.float64)
         out[s:s + m] = acc

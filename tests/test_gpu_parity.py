@@ -127,7 +127,7 @@ def test_visited_table_overflow_is_exact(gpu, oracle, spill_bits):
         np.testing.assert_array_equal(gd, od)
         assert s.get_last_search_dist_cmps() == o.get_last_search_dist_cmps()
     finally:
-        s.set_tuning(0, 0, 0, 1, 0)
+        s.set_tuning(0, 0, 0, 2, 0)
 
 
 def test_tuning_variants_agree(gpu, golden):
@@ -138,13 +138,15 @@ def test_tuning_variants_agree(gpu, golden):
     try:
         for wpb in (1, 2, 8):
             for lpr in (1, 2, 4):
-                for prefetch in (0, 1):
-                    s.set_tuning(warps_per_block=wpb, table_bits=0, lanes_per_row=lpr, prefetch=prefetch, spill_bits=0)
-                    ids, dis = s.batch_search(q, 10)
-                    np.testing.assert_array_equal(ids, ref_ids)
-                    np.testing.assert_array_equal(dis, ref_dis)
+                for prefetch in (0, 1, 2, 3):
+                    for bits in (0, 1, 9):  # automatic, global table only, 512 shared slots
+                        s.set_tuning(warps_per_block=wpb, table_bits=bits, lanes_per_row=lpr, prefetch=prefetch,
+                                     spill_bits=0)
+                        ids, dis = s.batch_search(q, 10)
+                        np.testing.assert_array_equal(ids, ref_ids)
+                        np.testing.assert_array_equal(dis, ref_dis)
     finally:
-        s.set_tuning(0, 0, 0, 1, 0)
+        s.set_tuning(0, 0, 0, 2, 0)
 
 
 def test_optimize_keeps_results(gpu):
@@ -158,7 +160,7 @@ def test_optimize_keeps_results(gpu):
     b = s.batch_search(q, 10)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
-    s.set_tuning(0, 0, 0, 1, 0)
+    s.set_tuning(0, 0, 0, 2, 0)
 
 
 def test_edge_inputs(gpu):
