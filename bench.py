@@ -208,6 +208,19 @@ def serving_leg(glass, s, queries):
             "at": "50% of saturation"}
 
 
+def replica_throughput(local_seconds, nq, steps, world, dist=None, device="cpu"):
+    """Whole-job QPS of `world` replicas that each searched nq queries per step: the slowest
+    rank's time bounds the job (max over ranks; no data is exchanged)."""
+    total = float(local_seconds)
+    if dist is not None and world > 1:
+        import torch
+
+        t = torch.tensor([total], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    return world * nq * steps / total, total
+
+
 def measured_peak():
     try:
         mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -309,12 +322,7 @@ def run_gpu(a):
     if a.profile:
         print(json.dumps({"profile": True, "ef": a.ef, "step_ms": step_ms, "tuning": tuning}))
         return
-    total_s = sum(step_ms) / 1000.0
-    if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * nq * a.steps / total_s
+    value, total_s = replica_throughput(sum(step_ms) / 1000.0, nq, a.steps, world, dist, "cuda")
     ms_per_step = 1000.0 * total_s / a.steps
 
     # algorithmic bytes of one launch: per query n_dist*csize + n_expand*4K + reorder_k rows of

@@ -54,16 +54,17 @@ void DevBuf::release() {
     bytes = 0;
 }
 
-int SpillTables::ensure(size_t n, int b, cudaStream_t st, int32_t **tab) {
-    const size_t bytes = n * ((size_t)1 << b) * 8;  // table + slot list per warp
+int SpillTables::ensure(size_t n, int b, cudaStream_t st, unsigned long long **tab, uint32_t **epoch) {
+    const size_t tbytes = n * ((size_t)1 << b) * 8;
     if (!buf.p || n != slots || b != bits) {
-        int rc = buf.ensure(bytes);
+        int rc = buf.ensure(tbytes + n * 4);
         if (rc) return rc;
-        GSX_CUDA(cudaMemsetAsync(buf.p, 0, bytes, st));
+        GSX_CUDA(cudaMemsetAsync(buf.p, 0, tbytes + n * 4, st));
         slots = n;
         bits = b;
     }
-    *tab = buf.as<int32_t>();
+    *tab = buf.as<unsigned long long>();
+    *epoch = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(buf.p) + tbytes);
     return GSX_OK;
 }
 
@@ -241,7 +242,7 @@ int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int3
     // one spill table per resident warp of this launch shape, 4x the shared table (>= 2^13 slots)
     const int sbits = spill_bits_for(s, cfg);
     const size_t slots = (size_t)cfg.max_blocks * cfg.warps_per_block;
-    if ((rc = s->spill.ensure(slots, sbits, st, &bv.gtab))) return rc;
+    if ((rc = s->spill.ensure(slots, sbits, st, &bv.gtab, &bv.gtab_epoch))) return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     return GSX_OK;
@@ -272,8 +273,9 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     const int slots_max = 16;
     cfg.blocks = std::max(1, std::min(((int)redo.size() + 3) / 4, slots_max / 4));
     const size_t slots = (size_t)cfg.blocks * cfg.warps_per_block;
-    int32_t *gt = nullptr;
-    if ((rc = s->gtab.ensure(slots, gbits, st, &gt))) return rc;
+    unsigned long long *gt = nullptr;
+    uint32_t *ge = nullptr;
+    if ((rc = s->gtab.ensure(slots, gbits, st, &gt, &ge))) return rc;
     if ((rc = upload(s->order, redo.data(), redo.size(), st))) return rc;
     if ((rc = s->status.ensure((size_t)nq * 4))) return rc;
     GSX_CUDA(cudaMemsetAsync(s->counters.p, 0, 8, st));
@@ -294,6 +296,7 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
     bv.gtab = gt;
+    bv.gtab_epoch = ge;
     bv.gtab_bits = gbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     GSX_CUDA(cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
@@ -676,7 +679,7 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
     if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
         return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
                     kMinTableBits);
-    if (t->prefetch < 0 || t->prefetch > 3) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 3]");
+    if (t->prefetch < 0 || t->prefetch > 7) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 7]");
     if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
         return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
     s->tuning = *t;
@@ -718,7 +721,7 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
     for (int wpb : {2, 4})
         for (int lpr : lprs)
             for (int bits : bit_choices)
-            for (int pf : {0, 1})
+            for (int pf : {0, 4})
             for (int sb : {auto_sb, auto_sb + 1}) {
                 gsx_tuning t{wpb, bits, lpr, pf, sb};
                 s->tuning = t;

@@ -40,8 +40,8 @@ int validate_graph(const HostGraph &g);
 
 // A device allocation that grows on demand.
 struct DevBuf;
-// Global visited tables of `slots` warps: per warp 2^bits int32 table slots then a list of as many
-// int32; zeroed whenever the layout changes (the kernel keeps them all-zero between queries).
+// Global visited tables of `slots` warps (2^bits 64-bit entries each) followed by their epoch
+// counters; zeroed whenever the layout changes, so every slot reads as empty and epochs restart.
 struct SpillTables;
 struct DevBuf {
     void *p = nullptr;
@@ -57,7 +57,7 @@ struct SpillTables {
     DevBuf buf;
     size_t slots = 0;
     int bits = 0;
-    int ensure(size_t slots, int bits, cudaStream_t st, int32_t **tab);
+    int ensure(size_t slots, int bits, cudaStream_t st, unsigned long long **tab, uint32_t **epoch);
 };
 
 }  // namespace gsx

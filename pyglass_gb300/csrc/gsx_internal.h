@@ -17,6 +17,8 @@ constexpr int kMinTableBits = 7;     // smallest visited table: 128 slots
 constexpr int kGlobalOnly = 1;       // table_bits value: no shared table, visited set in global memory
 constexpr int kPrefetchCodes = 1;    // tuning.prefetch bit: L1 prefetch of the predicted row's codes
 constexpr int kSpeculateRow = 2;     // tuning.prefetch bit: load the predicted next row during the merge
+constexpr int kPrefetchNeighbours = 4;  // tuning.prefetch bit: L1 prefetch of each neighbour's codes
+                                        // before its visited check
 
 // Device-resident index, as the kernels see it.
 struct IndexView {
@@ -54,9 +56,8 @@ struct BatchView {
     int32_t *status;          // per-query: 0 ok, 1 visited table full (query left unanswered)
     unsigned int *counter;    // work-queue head, zeroed before the launch
     unsigned int *overflow;   // number of overflowed queries
-    int32_t *gtab;            // optional global visited tables: per warp slot 2^gtab_bits slots
-                              // (id + 1, zero when empty) then a list of as many filled slots;
-                              // all-zero between queries
+    unsigned long long *gtab; // optional global visited tables (epoch << 32 | id), one per warp slot
+    uint32_t *gtab_epoch;     // their epoch counters (zero-initialised)
     int32_t gtab_bits;
 };
 

@@ -37,14 +37,12 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 
 // Visited set, open addressing with linear probing.  Two storages share the probe sequence:
 //  * the shared-memory table: 2^bits int32 slots, -1 = empty, cleared for every query;
-//  * the warp's global table: 2^bits int32 slots holding id + 1, 0 = empty.  It is all-zero
-//    between queries: each query appends the slots it fills to the warp's slot list and zeroes
-//    them when it ends, so a single atomicCAS both tests and inserts (one L2 round trip).
-// Probing is bounded by the table size; the caller keeps the load under 3/4 so a free slot always
-// exists.
+//  * the warp's global spill table: 2^bits uint64 slots holding (epoch << 32 | id), where a slot
+//    is empty unless its epoch is the query's own, so it is never cleared (epochs only grow).
+// Returns true if v was absent (and is now present).  Probing is bounded by the table size; the
+// caller keeps the load under 3/4 so a free slot always exists.
 __device__ __forceinline__ uint32_t slot_of(int32_t v, int bits) { return ((uint32_t)v * 0x9E3779B1u) >> (32 - bits); }
 
-// true if v was absent (and is now present)
 __device__ __forceinline__ bool visit_shared(int32_t *tab, int bits, int32_t v) {
     const uint32_t mask = (1u << bits) - 1u;
     uint32_t h = slot_of(v, bits);
@@ -57,16 +55,23 @@ __device__ __forceinline__ bool visit_shared(int32_t *tab, int bits, int32_t v) 
     return false;
 }
 
-// The slot v was inserted into (probing from slot h), or -1 if v was present.
-__device__ __forceinline__ int visit_global(int32_t *tab, int bits, int32_t v, uint32_t h) {
+__device__ __forceinline__ bool visit_global(unsigned long long *tab, int bits, uint32_t epoch, int32_t v) {
     const uint32_t mask = (1u << bits) - 1u;
-    for (uint32_t p = 0; p <= mask; ++p) {
-        const int32_t old = atomicCAS(tab + h, 0, v + 1);
-        if (old == 0) return (int)h;
-        if (old == v + 1) return -1;
-        h = (h + 1u) & mask;
+    const unsigned long long mine = ((unsigned long long)epoch << 32) | (uint32_t)v;
+    uint32_t h = slot_of(v, bits);
+    for (uint32_t p = 0; p <= mask;) {
+        const unsigned long long cur = *((volatile unsigned long long *)(tab + h));
+        if ((uint32_t)(cur >> 32) == epoch) {
+            if ((uint32_t)cur == (uint32_t)v) return false;
+            h = (h + 1u) & mask;
+            ++p;
+            continue;
+        }
+        const unsigned long long old = atomicCAS(tab + h, cur, mine);
+        if (old == cur) return true;
+        // another lane of this warp filled the slot first: look at it again
     }
-    return -1;
+    return false;
 }
 
 // First index in [lo, hi) whose entry is not yet expanded, or hi.
@@ -99,70 +104,58 @@ struct WarpState {
     int32_t *acc_id;
     float *fq;
     uint32_t *qc;
-    int32_t *tab;                // shared-memory table
+    int32_t *tab;                // shared-memory table (null when the query runs on the spill table)
     int tbits;
-    int32_t *spill;              // this warp's global table (zero between queries), or null
-    int32_t *slist;              // slots of the global table the current query filled
+    unsigned long long *spill;   // this warp's global table (epoch-tagged), or null
+    uint32_t *spill_epoch;       // its epoch counter
     int sbits;
-    int nlist;                   // entries in slist
-    bool global;                 // the current query's visited set is in the global table
+    uint32_t epoch;              // epoch of the current query in the spill table (0 = not used)
     bool shared_first;           // queries start in the shared-memory table
 };
 
-// Inserts v (each lane its own id, all lanes calling); returns true if v was absent.  Global-table
-// slots filled by this call are appended to the warp's slot list.
-__device__ __forceinline__ bool visit(WarpState &w, int32_t v, bool active, int lane) {
-    if (!w.global) return active && visit_shared(w.tab, w.tbits, v);
-    const int slot = active ? visit_global(w.spill, w.sbits, v, slot_of(v, w.sbits)) : -1;
-    const unsigned fm = __ballot_sync(kFull, slot >= 0);
-    if (slot >= 0) w.slist[w.nlist + __popc(fm & ((1u << lane) - 1u))] = slot;
-    w.nlist += __popc(fm);
-    return slot >= 0;
+__device__ __forceinline__ bool visit(WarpState &w, int32_t v) {
+    return w.epoch ? visit_global(w.spill, w.sbits, w.epoch, v) : visit_shared(w.tab, w.tbits, v);
 }
 
-// Zeroes the global-table slots the query filled, leaving the table all-zero for the next query.
-__device__ __forceinline__ void visited_release(WarpState &w, int lane) {
-    if (!w.global) return;
-    __syncwarp();
-    for (int i = lane; i < w.nlist; i += 32) w.spill[w.slist[i]] = 0;
-    __syncwarp();
-    __threadfence_block();
-    w.nlist = 0;
+// Starts a fresh epoch of the warp's spill table for the current query.
+__device__ __forceinline__ void spill_begin(WarpState &w, int lane) {
+    uint32_t e = 0;
+    if (lane == 0) e = atomicAdd(w.spill_epoch, 1u) + 1u;
+    w.epoch = __shfl_sync(kFull, e, 0);
 }
 
-// Moves the visited set from the shared-memory table into the warp's global table and continues
-// there: the set is unchanged, only its storage grows.  Each lane re-inserts its share of the
-// slots; first probes are issued eight at a time so that their latencies overlap.
+// Moves the visited set from the shared-memory table into the warp's global spill table under a
+// fresh epoch and continues there: the set is unchanged, only its storage grows.  Each lane
+// re-inserts its share of the slots; first probes are issued eight at a time so that their
+// latencies overlap.
 __device__ __forceinline__ void migrate_visited(WarpState &w, int lane) {
+    spill_begin(w, lane);
     const int tsize = 1 << w.tbits;
-    w.global = true;
-    w.nlist = 0;
-    for (int j0 = 0; j0 < tsize; j0 += 32 * 8) {
+    const uint32_t mask = (1u << w.sbits) - 1u;
+    for (int j0 = lane; j0 < tsize; j0 += 32 * 8) {
         int32_t v[8];
-        int slot[8];
+        unsigned long long old[8];
+        uint32_t h[8];
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
-            const int j = j0 + 32 * t + lane;
+            const int j = j0 + 32 * t;
             v[t] = j < tsize ? w.tab[j] : -1;
+            h[t] = v[t] != -1 ? slot_of(v[t], w.sbits) : 0u;
         }
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
-            slot[t] = -1;
+            old[t] = 0;
             if (v[t] != -1) {
-                const uint32_t h = slot_of(v[t], w.sbits);
-                slot[t] = atomicCAS(w.spill + h, 0, v[t] + 1) == 0 ? (int)h : -2;
+                const unsigned long long cur = *((volatile unsigned long long *)(w.spill + h[t]));
+                old[t] = (uint32_t)(cur >> 32) == w.epoch ? cur : atomicCAS(w.spill + h[t], cur, ((unsigned long long)w.epoch << 32) | (uint32_t)v[t]);
+                // the slot was ours to take when the CAS saw the value read
+                if ((uint32_t)(cur >> 32) != w.epoch && old[t] == cur) v[t] = -1;
             }
         }
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            if (slot[t] == -2) {  // first slot taken: keep probing
-                const uint32_t h = (slot_of(v[t], w.sbits) + 1u) & ((1u << w.sbits) - 1u);
-                slot[t] = visit_global(w.spill, w.sbits, v[t], h);
-            }
-            const unsigned fm = __ballot_sync(kFull, slot[t] >= 0);
-            if (slot[t] >= 0) w.slist[w.nlist + __popc(fm & ((1u << lane) - 1u))] = slot[t];
-            w.nlist += __popc(fm);
-        }
+        for (int t = 0; t < 8; ++t)
+            if (v[t] != -1) visit_global(w.spill, w.sbits, w.epoch, v[t]);
+        (void)mask;
     }
     __syncwarp();
 }
@@ -394,18 +387,17 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
     __syncwarp();
     const int32_t qsq = prepare_query<KIND, METRIC>(ix, w, lane);
 
-    // visited set: a cleared shared-memory table, or (when the launch has none) the warp's global
-    // table, which the previous query left all-zero
+    // visited set: a cleared shared-memory table, or (when the launch has none) a fresh epoch of the
+    // warp's global table
     int tlimit;
-    w.nlist = 0;
     if (w.shared_first) {
-        w.global = false;
+        w.epoch = 0;
         const int tsize = 1 << w.tbits;
         for (int j = lane * 4; j < tsize; j += 128) *reinterpret_cast<int4 *>(w.tab + j) = make_int4(-1, -1, -1, -1);
         __syncwarp();
         tlimit = (tsize >> 2) * 3;
     } else {
-        w.global = true;
+        spill_begin(w, lane);
         tlimit = ((1 << w.sbits) >> 2) * 3;
     }
 
@@ -470,7 +462,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         __syncwarp();
         merge(w, S, cap, lb, 1, lane);
-        visit(w, u, lane == 0, lane);
+        if (lane == 0) visit(w, u);
         nvis += 1;
         __syncwarp();
     } else {
@@ -481,7 +473,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
             cmps += m;
             merge(w, S, cap, lb, m, lane);
-            for (int j0 = 0; j0 < m; j0 += 32) visit(w, w.cand_id[j0 + lane < m ? j0 + lane : 0], j0 + lane < m, lane);
+            for (int j = lane; j < m; j += 32) visit(w, w.cand_id[j]);
             nvis += m;
             __syncwarp();
             if (nvis > tlimit) { overflow = true; break; }
@@ -496,7 +488,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         const int f = first_unchecked(w.pid, lb, S < lim ? S : lim, lane);
         if (f >= S || f >= lim) break;
         if (nvis + ix.K > tlimit) {
-            if (w.spill && !w.global) {
+            if (w.spill && w.epoch == 0) {
                 migrate_visited(w, lane);
                 tlimit = ((1 << w.sbits) >> 2) * 3;
             }
@@ -524,7 +516,13 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             const unsigned same = __match_any_sync(kFull, v);
             const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
             const bool first = valid && ((same & vmask & lanemask_lt()) == 0);
-            const bool fresh = visit(w, v, first, lane);
+            if ((L.prefetch & kPrefetchNeighbours) && first) {
+                // start the code row's way into L1 now, so that it overlaps the visited check
+                const uint8_t *c = ix.codes + (size_t)v * (size_t)ix.csize;
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(c));
+                if (ix.csize > 128) asm volatile("prefetch.global.L1 [%0];" ::"l"(c + 128));
+            }
+            const bool fresh = first && visit(w, v);
             const unsigned nm = __ballot_sync(kFull, fresh);
             if (fresh) w.cand_id[m + __popc(nm & lanemask_lt())] = v;
             m += __popc(nm);
@@ -561,8 +559,6 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             }
         }
     }
-
-    visited_release(w, lane);
 
     // ---- results ----
     int32_t *oid = bv.out_ids + (size_t)qi * (size_t)bv.out_stride;
@@ -652,12 +648,10 @@ __global__ void __launch_bounds__(256) search_kernel(IndexView ix, BatchView bv,
     w.fq = reinterpret_cast<float *>(ws + L.fq);
     w.qc = reinterpret_cast<uint32_t *>(ws + L.qc);
     const size_t slot = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
-    // per warp slot: the table (2^bits int32) followed by its slot list (2^bits int32)
-    w.spill = bv.gtab ? bv.gtab + (slot << (bv.gtab_bits + 1)) : nullptr;
-    w.slist = bv.gtab ? w.spill + ((size_t)1 << bv.gtab_bits) : nullptr;
+    w.spill = bv.gtab ? bv.gtab + (slot << bv.gtab_bits) : nullptr;
+    w.spill_epoch = bv.gtab ? bv.gtab_epoch + slot : nullptr;
     w.sbits = bv.gtab_bits;
-    w.nlist = 0;
-    w.global = false;
+    w.epoch = 0;
     w.shared_first = L.table_bits > 0;
     w.tab = reinterpret_cast<int32_t *>(ws + L.table);
     w.tbits = L.table_bits;
