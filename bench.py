@@ -38,7 +38,7 @@ K = 10
 def args_():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--ef", type=int, default=128)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -115,46 +115,68 @@ def cpu_baseline(base, queries, ef, sample):
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region: the sampler
+    starts before the region (the region begins once its first sample has arrived) and only the
+    samples taken inside the region are summarised."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 20
 
     def __init__(self, dev):
         self.dev = dev
         self.p = None
+        self.rows = []
+        self.t0 = self.t1 = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                self.rows.append((time.perf_counter(), f))
 
     def __enter__(self):
+        import threading
+
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
-                                      stderr=subprocess.DEVNULL, text=True)
+                                       "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
         except OSError:
             self.p = None
+        if self.p is not None:
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+            deadline = time.perf_counter() + 10
+            while not self.rows and time.perf_counter() < deadline and self.p.poll() is None:
+                time.sleep(0.005)
+        self.t0 = time.perf_counter()
         return self
 
     def __exit__(self, *a):
-        self.rows = []
+        self.t1 = time.perf_counter()
         if self.p is None:
             return
-        time.sleep(0.3)
+        time.sleep(2 * self.PERIOD_MS / 1000)
         self.p.terminate()
-        out, _ = self.p.communicate(timeout=10)
-        for line in out.strip().splitlines():
-            f = [x.strip() for x in line.split(",")]
-            if len(f) >= 9:
-                self.rows.append(f)
+        try:
+            self.p.wait(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.th.join(timeout=5)
 
     def summary(self):
-        if not getattr(self, "rows", None):
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        inside = [f for t, f in self.rows if self.t0 is not None and self.t0 <= t <= self.t1 + self.PERIOD_MS / 1000]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        num = lambda x: x.replace(".", "", 1).isdigit()
+        sm = [float(r[1]) for r in inside if num(r[1])]
+        mx = [float(r[2]) for r in inside if num(r[2])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in inside for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(inside), "region_s": round(self.t1 - self.t0, 3)}
 
 
 def ground_truth(torch, glass, base_t, q_t, k):
@@ -227,6 +249,18 @@ def measured_peak():
         return float(mp["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def profiled_traffic(ef):
+    """DRAM bytes (read + write) of one search launch from the committed ncu summary of this
+    workload, or None when there is none for this ef."""
+    import re
+
+    path = os.path.join(ROOT, "profiles", f"search_sq4u_{WORKLOAD}_ef{ef}.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic per launch[^|]*\|\s*([0-9.]+) GB", open(path).read())
+    return float(m.group(1)) * 1e9 if m else None
 
 
 def run_reference(a):
@@ -334,10 +368,7 @@ def run_gpu(a):
     kern_s = statistics.mean(step_ms) / 1000.0
     peak, peak_kind = measured_peak()
     achieved = alg_bytes / kern_s / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get(f"search_sq4u_{WORKLOAD}_ef{a.ef}")
+    traffic = profiled_traffic(a.ef)
 
     out_ids = ids.cpu().numpy()
     base_t = torch.from_numpy(base).cuda()

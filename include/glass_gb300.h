@@ -143,10 +143,14 @@ typedef struct {
     int32_t table_bits;       /* log2 of the per-query visited-table slots in shared memory
                                  (1 = none: the visited set lives in the warp's global table) */
     int32_t lanes_per_row;    /* lanes cooperating on one code row (SQ kinds) */
-    int32_t prefetch;         /* bit 2: prefetch each neighbour's code row into L1 before its
-                                 visited check; bit 1: load the predicted next adjacency row
-                                 during the merge; bit 0: also prefetch that row's code rows */
-    int32_t spill_bits;       /* log2 of the per-warp global table a full shared table spills into */
+    int32_t prefetch;         /* bit 3: do not stage neighbour code rows in shared memory during
+                                 the visited check (staging applies to SQ8U/SQ4U rows of at most
+                                 128 bytes); bit 2: prefetch each neighbour's code row into L1
+                                 before its visited check (unstaged rows); bit 1: load the
+                                 predicted next adjacency row during the merge; bit 0: also
+                                 prefetch that row's code rows */
+    int32_t spill_bits;       /* log2 of the slots of each warp's global visited table (4 bytes a
+                                 slot; 7..20, 0 = sized from the visit counts seen) */
 } gsx_tuning;
 int gsx_searcher_get_tuning(const gsx_searcher *s, gsx_tuning *t);
 int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t);

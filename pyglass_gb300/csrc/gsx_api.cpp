@@ -54,16 +54,17 @@ void DevBuf::release() {
     bytes = 0;
 }
 
-int SpillTables::ensure(size_t n, int b, cudaStream_t st, unsigned long long **tab, uint32_t **epoch) {
-    const size_t tbytes = n * ((size_t)1 << b) * 8;
-    if (!buf.p || n != slots || b != bits) {
+int SpillTables::ensure(size_t n, int b, int sh, cudaStream_t st, uint32_t **tab, uint32_t **epoch) {
+    const size_t tbytes = n * ((size_t)1 << b) * 4;
+    if (!buf.p || n != slots || b != bits || sh != shift) {
         int rc = buf.ensure(tbytes + n * 4);
         if (rc) return rc;
         GSX_CUDA(cudaMemsetAsync(buf.p, 0, tbytes + n * 4, st));
         slots = n;
         bits = b;
+        shift = sh;
     }
-    *tab = buf.as<unsigned long long>();
+    *tab = buf.as<uint32_t>();
     *epoch = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(buf.p) + tbytes);
     return GSX_OK;
 }
@@ -195,16 +196,17 @@ int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int tabl
     return GSX_OK;
 }
 
-// Global (spill) table size.  Every probe past the first costs another L2 round trip, so the table
-// is kept sparse: about 8x the largest visit count seen on this searcher (12% load), 2^14..2^17
-// slots.
+// Global visited-table size (4 bytes a slot, read in 32-byte buckets): the largest visit count
+// seen on this searcher with 25% headroom (before any batch: half of ef*K), at the kernel's 7/8
+// load limit, then one size up so that buckets rarely fill, 2^11..2^20 slots.  A query that still
+// outgrows it is re-run by resolve_overflow.
 int spill_bits_for(const gsx_searcher *s, const LaunchCfg &cfg) {
-    (void)cfg;
     if (s->tuning.spill_bits > 0) return s->tuning.spill_bits;
-    int bits = 14;
-    const int64_t want = s->visit_hint > 0 ? (int64_t)s->visit_hint * 8 : 0;
-    while ((1ll << bits) < want && bits < 17) ++bits;
-    return bits;
+    const int64_t want = s->visit_hint > 0 ? (int64_t)s->visit_hint * 5 / 4 + s->ix.K
+                                           : (int64_t)cfg.L.cap * s->ix.K / 2;
+    int bits = 10;
+    while ((1ll << bits) - ((1ll << bits) >> 3) < want && bits < 19) ++bits;
+    return bits + 1;
 }
 
 // Enqueues one batch on `st`; nothing is synchronised.
@@ -239,10 +241,11 @@ int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int3
     bv.status = s->status.as<int32_t>();
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
-    // one spill table per resident warp of this launch shape, 4x the shared table (>= 2^13 slots)
+    // one global visited table per resident warp of this launch shape
     const int sbits = spill_bits_for(s, cfg);
     const size_t slots = (size_t)cfg.max_blocks * cfg.warps_per_block;
-    if ((rc = s->spill.ensure(slots, sbits, st, &bv.gtab, &bv.gtab_epoch))) return rc;
+    bv.gtab_shift = visited_id_bits(s->ix.N);
+    if ((rc = s->spill.ensure(slots, sbits, bv.gtab_shift, st, &bv.gtab, &bv.gtab_epoch))) return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     return GSX_OK;
@@ -273,9 +276,9 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     const int slots_max = 16;
     cfg.blocks = std::max(1, std::min(((int)redo.size() + 3) / 4, slots_max / 4));
     const size_t slots = (size_t)cfg.blocks * cfg.warps_per_block;
-    unsigned long long *gt = nullptr;
-    uint32_t *ge = nullptr;
-    if ((rc = s->gtab.ensure(slots, gbits, st, &gt, &ge))) return rc;
+    uint32_t *gt = nullptr, *ge = nullptr;
+    const int shift = visited_id_bits(s->ix.N);
+    if ((rc = s->gtab.ensure(slots, gbits, shift, st, &gt, &ge))) return rc;
     if ((rc = upload(s->order, redo.data(), redo.size(), st))) return rc;
     if ((rc = s->status.ensure((size_t)nq * 4))) return rc;
     GSX_CUDA(cudaMemsetAsync(s->counters.p, 0, 8, st));
@@ -298,6 +301,7 @@ int resolve_overflow(gsx_searcher *s, const float *d_q, int nq, int k, int ef, c
     bv.gtab = gt;
     bv.gtab_epoch = ge;
     bv.gtab_bits = gbits;
+    bv.gtab_shift = shift;
     GSX_CUDA(launch_search(s->ix, bv, cfg, st));
     GSX_CUDA(cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
     GSX_CUDA(cudaStreamSynchronize(st));
@@ -679,7 +683,7 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
     if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
         return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
                     kMinTableBits);
-    if (t->prefetch < 0 || t->prefetch > 7) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 7]");
+    if (t->prefetch < 0 || t->prefetch > 15) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 15]");
     if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
         return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
     s->tuning = *t;

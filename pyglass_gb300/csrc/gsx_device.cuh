@@ -147,6 +147,53 @@ __device__ __forceinline__ int32_t sq_partial(const uint8_t *__restrict__ codes,
     }
 }
 
+// Whole-row integer partial distance (one lane per row) from a row in shared memory: the same
+// arithmetic as sq_partial with one lane.
+template <int KIND, int METRIC>
+__device__ __forceinline__ int32_t sq_partial_row(const uint4 *row, int nch, const uint32_t *qc) {
+    if (KIND == K_SQ4U) {
+        const uint4 *ql = reinterpret_cast<const uint4 *>(qc);
+        const uint4 *qh = reinterpret_cast<const uint4 *>(qc + 4 * nch);
+        uint32_t aa = 0, ab = 0;
+#pragma unroll 4
+        for (int c = 0; c < nch; ++c) {
+            const uint4 v = row[c];
+            const uint4 l = ql[c], h = qh[c];
+            sq4_word(v.x, l.x, h.x, aa, ab);
+            sq4_word(v.y, l.y, h.y, aa, ab);
+            sq4_word(v.z, l.z, h.z, aa, ab);
+            sq4_word(v.w, l.w, h.w, aa, ab);
+        }
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (METRIC == M_L2) {
+        const uint4 *qv = reinterpret_cast<const uint4 *>(qc);
+        uint32_t aa = 0, ab = 0;
+#pragma unroll 4
+        for (int c = 0; c < nch; ++c) {
+            const uint4 v = row[c];
+            const uint4 q = qv[c];
+            aa = __dp4a(v.x, v.x, aa); ab = __dp4a(v.x, q.x, ab);
+            aa = __dp4a(v.y, v.y, aa); ab = __dp4a(v.y, q.y, ab);
+            aa = __dp4a(v.z, v.z, aa); ab = __dp4a(v.z, q.z, ab);
+            aa = __dp4a(v.w, v.w, aa); ab = __dp4a(v.w, q.w, ab);
+        }
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else {
+        const uint4 *qv = reinterpret_cast<const uint4 *>(qc);
+        int32_t s = 0;
+#pragma unroll 4
+        for (int c = 0; c < nch; ++c) {
+            const uint4 v = row[c];
+            const uint4 q = qv[c];
+            s = __dp4a((int)v.x, (int)q.x, s);
+            s = __dp4a((int)v.y, (int)q.y, s);
+            s = __dp4a((int)v.z, (int)q.z, s);
+            s = __dp4a((int)v.w, (int)q.w, s);
+        }
+        return s;
+    }
+}
+
 // Finishes a team's integer distance (all lanes of the warp must call it).
 template <int KIND, int METRIC, int LPR>
 __device__ __forceinline__ int32_t sq_finish(int32_t partial, int32_t qsq) {

@@ -40,8 +40,9 @@ int validate_graph(const HostGraph &g);
 
 // A device allocation that grows on demand.
 struct DevBuf;
-// Global visited tables of `slots` warps (2^bits 64-bit entries each) followed by their epoch
-// counters; zeroed whenever the layout changes, so every slot reads as empty and epochs restart.
+// Global visited tables of `slots` warps (2^bits 32-bit entries each) followed by their query
+// counters; zeroed whenever the layout (slots, bits, id bits) changes, so every slot reads as
+// empty and the counters restart.
 struct SpillTables;
 struct DevBuf {
     void *p = nullptr;
@@ -57,7 +58,8 @@ struct SpillTables {
     DevBuf buf;
     size_t slots = 0;
     int bits = 0;
-    int ensure(size_t slots, int bits, cudaStream_t st, unsigned long long **tab, uint32_t **epoch);
+    int shift = 0;
+    int ensure(size_t slots, int bits, int shift, cudaStream_t st, uint32_t **tab, uint32_t **epoch);
 };
 
 }  // namespace gsx

@@ -19,6 +19,8 @@ constexpr int kPrefetchCodes = 1;    // tuning.prefetch bit: L1 prefetch of the 
 constexpr int kSpeculateRow = 2;     // tuning.prefetch bit: load the predicted next row during the merge
 constexpr int kPrefetchNeighbours = 4;  // tuning.prefetch bit: L1 prefetch of each neighbour's codes
                                         // before its visited check
+constexpr int kNoStageCodes = 8;     // tuning.prefetch bit: do not stage neighbour code rows in shared
+                                     // memory during the visited check (SQ kinds, rows <= 128 bytes)
 
 // Device-resident index, as the kernels see it.
 struct IndexView {
@@ -56,14 +58,26 @@ struct BatchView {
     int32_t *status;          // per-query: 0 ok, 1 visited table full (query left unanswered)
     unsigned int *counter;    // work-queue head, zeroed before the launch
     unsigned int *overflow;   // number of overflowed queries
-    unsigned long long *gtab; // optional global visited tables (epoch << 32 | id), one per warp slot
-    uint32_t *gtab_epoch;     // their epoch counters (zero-initialised)
+    uint32_t *gtab;           // optional global visited tables, one per warp slot: 2^gtab_bits
+                              // slots of (tag << gtab_shift | id), tag 1..2^(32-gtab_shift)-1
+    uint32_t *gtab_epoch;     // their query counters (zero-initialised)
     int32_t gtab_bits;
+    int32_t gtab_shift;       // id bits of the graph (visited_id_bits(N))
 };
+
+// Bits that hold every node id of an n-node graph in a global visited-table slot; the remaining
+// high bits tag the query that wrote the slot.
+inline int visited_id_bits(int64_t n) {
+    int b = 1;
+    while (b < 31 && (1ll << b) < n) ++b;
+    return b;
+}
 
 // Byte offsets of one warp's slice of dynamic shared memory.
 struct WarpLayout {
     int pool_key, pool_id, cand_id, cand_key, acc_ub, acc_key, acc_id, fq, qc, table;
+    int stage;                // 32 code rows staged by cp.async (byte offset), when stage_row > 0
+    int stage_row;            // bytes per staged row (the code size), 0 = no staging
     int total;                // bytes per warp (multiple of 16)
     int cap;                  // pool capacity available
     int fq_len;               // floats in the fp32 query buffer

@@ -200,7 +200,9 @@ int launch_group(gsx_server *sv, Group *g, int si) {
     bv.status = sv->dstatus.as<int32_t>();
     bv.counter = cnt;
     bv.overflow = cnt + 1;
-    if ((rc = sv->spill[si]->ensure((size_t)cfg.max_blocks * cfg.warps_per_block, sbits, st, &bv.gtab, &bv.gtab_epoch)))
+    bv.gtab_shift = visited_id_bits(sv->s->ix.N);
+    if ((rc = sv->spill[si]->ensure((size_t)cfg.max_blocks * cfg.warps_per_block, sbits, bv.gtab_shift, st, &bv.gtab,
+                                    &bv.gtab_epoch)))
         return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(sv->s->ix, bv, cfg, st));

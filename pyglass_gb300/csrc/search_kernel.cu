@@ -35,14 +35,19 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Visited set, open addressing with linear probing.  Two storages share the probe sequence:
-//  * the shared-memory table: 2^bits int32 slots, -1 = empty, cleared for every query;
-//  * the warp's global spill table: 2^bits uint64 slots holding (epoch << 32 | id), where a slot
-//    is empty unless its epoch is the query's own, so it is never cleared (epochs only grow).
-// Returns true if v was absent (and is now present).  Probing is bounded by the table size; the
-// caller keeps the load under 3/4 so a free slot always exists.
+// Visited set, open addressing.  Two storages:
+//  * the shared-memory table: 2^bits int32 slots, -1 = empty, linear probing, cleared for every
+//    query;
+//  * the warp's global table: 2^bits uint32 slots in buckets of eight (one 32-byte load reads a
+//    bucket), probed bucket after bucket.  A slot holds (tag << shift | id), shift = the graph's id
+//    bits; it is empty unless its tag is the current query's.  Tags run 1..2^(32-shift)-1 over
+//    the warp's successive queries and the table is cleared only when they wrap, so a query
+//    starts on a clean table without writing it.
+// Probing is bounded by the table size; the caller keeps the load under 3/4 (shared) or 7/8
+// (global) so a free slot always exists.
 __device__ __forceinline__ uint32_t slot_of(int32_t v, int bits) { return ((uint32_t)v * 0x9E3779B1u) >> (32 - bits); }
 
+// Returns true if v was absent (and is now present).
 __device__ __forceinline__ bool visit_shared(int32_t *tab, int bits, int32_t v) {
     const uint32_t mask = (1u << bits) - 1u;
     uint32_t h = slot_of(v, bits);
@@ -55,24 +60,48 @@ __device__ __forceinline__ bool visit_shared(int32_t *tab, int bits, int32_t v) 
     return false;
 }
 
-__device__ __forceinline__ bool visit_global(unsigned long long *tab, int bits, uint32_t epoch, int32_t v) {
-    const uint32_t mask = (1u << bits) - 1u;
-    const unsigned long long mine = ((unsigned long long)epoch << 32) | (uint32_t)v;
-    uint32_t h = slot_of(v, bits);
-    for (uint32_t p = 0; p <= mask;) {
-        const unsigned long long cur = *((volatile unsigned long long *)(tab + h));
-        if ((uint32_t)(cur >> 32) == epoch) {
-            if ((uint32_t)cur == (uint32_t)v) return false;
-            h = (h + 1u) & mask;
-            ++p;
-            continue;
-        }
-        const unsigned long long old = atomicCAS(tab + h, cur, mine);
-        if (old == cur) return true;
-        // another lane of this warp filled the slot first: look at it again
-    }
-    return false;
+struct Bucket {
+    uint32_t e[8];
+};
+
+// One 32-byte bucket (an L2 sector) in one load.  Plain (weak, L1-cached) loads and stores are
+// enough: a table is used by one warp only, and within a launch a warp stays on one SM, so its
+// lanes' accesses are ordered by __syncwarp.  No atomics touch the global tables.
+__device__ __forceinline__ Bucket load_bucket(const uint32_t *p) {
+    Bucket b;
+    asm volatile("ld.global.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(b.e[0]), "=r"(b.e[1]), "=r"(b.e[2]), "=r"(b.e[3]), "=r"(b.e[4]), "=r"(b.e[5]), "=r"(b.e[6]),
+                   "=r"(b.e[7])
+                 : "l"(p)
+                 : "memory");
+    return b;
 }
+
+__device__ __forceinline__ void store_slot(uint32_t *p, uint32_t v) {
+    asm volatile("st.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr int kBucketFull = 16;
+
+// Slot of the first match or free slot in a bucket: 0..7 = a free slot, 8..15 = v found (8 +
+// slot), kBucketFull = the bucket holds eight other ids.  Inserts take the first free slot along
+// the probe sequence and slots are never freed under one tag, so a free slot before v means v
+// is absent.
+__device__ __forceinline__ int scan_bucket(const Bucket &b, uint32_t mine, int shift, uint32_t tag) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (b.e[j] == mine) return 8 + j;
+        if ((b.e[j] >> shift) != tag) return j;
+    }
+    return kBucketFull;
+}
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // First index in [lo, hi) whose entry is not yet expanded, or hi.
 __device__ __forceinline__ int first_unchecked(const int32_t *pid, int lo, int hi, int lane) {
@@ -104,59 +133,156 @@ struct WarpState {
     int32_t *acc_id;
     float *fq;
     uint32_t *qc;
+    unsigned char *stage;        // staged code rows (one per lane)
     int32_t *tab;                // shared-memory table (null when the query runs on the spill table)
     int tbits;
-    unsigned long long *spill;   // this warp's global table (epoch-tagged), or null
-    uint32_t *spill_epoch;       // its epoch counter
+    uint32_t *spill;             // this warp's global table (tagged slots), or null
+    uint32_t *spill_epoch;       // its query counter
     int sbits;
-    uint32_t epoch;              // epoch of the current query in the spill table (0 = not used)
+    int shift;                   // id bits of a global-table slot
+    uint32_t epoch;              // tag of the current query in the global table (0 = not used)
     bool shared_first;           // queries start in the shared-memory table
 };
 
-__device__ __forceinline__ bool visit(WarpState &w, int32_t v) {
-    return w.epoch ? visit_global(w.spill, w.sbits, w.epoch, v) : visit_shared(w.tab, w.tbits, v);
-}
-
-// Starts a fresh epoch of the warp's spill table for the current query.
-__device__ __forceinline__ void spill_begin(WarpState &w, int lane) {
-    uint32_t e = 0;
-    if (lane == 0) e = atomicAdd(w.spill_epoch, 1u) + 1u;
-    w.epoch = __shfl_sync(kFull, e, 0);
-}
-
-// Moves the visited set from the shared-memory table into the warp's global spill table under a
-// fresh epoch and continues there: the set is unchanged, only its storage grows.  Each lane
-// re-inserts its share of the slots; first probes are issued eight at a time so that their
-// latencies overlap.
-__device__ __forceinline__ void migrate_visited(WarpState &w, int lane) {
-    spill_begin(w, lane);
-    const int tsize = 1 << w.tbits;
-    const uint32_t mask = (1u << w.sbits) - 1u;
-    for (int j0 = lane; j0 < tsize; j0 += 32 * 8) {
-        int32_t v[8];
-        unsigned long long old[8];
-        uint32_t h[8];
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int j = j0 + 32 * t;
-            v[t] = j < tsize ? w.tab[j] : -1;
-            h[t] = v[t] != -1 ? slot_of(v[t], w.sbits) : 0u;
-        }
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            old[t] = 0;
-            if (v[t] != -1) {
-                const unsigned long long cur = *((volatile unsigned long long *)(w.spill + h[t]));
-                old[t] = (uint32_t)(cur >> 32) == w.epoch ? cur : atomicCAS(w.spill + h[t], cur, ((unsigned long long)w.epoch << 32) | (uint32_t)v[t]);
-                // the slot was ours to take when the CAS saw the value read
-                if ((uint32_t)(cur >> 32) != w.epoch && old[t] == cur) v[t] = -1;
+// Warp-wide visited check in the global table, one candidate per lane (`want`): one bucket load
+// per lane, then plain stores, since the table belongs to this warp alone.  Lanes that pick the
+// same free slot are ordered by lane: the lowest one stores, the others read the bucket again after
+// the store.  Returns true where v was absent (and is now present).  `bad` is set if a lane's probe
+// went round the whole table (cannot happen under the load limit).
+__device__ __forceinline__ bool visit_global_warp(WarpState &w, bool want, int32_t v, bool &bad) {
+    const uint32_t mine = (w.epoch << w.shift) | (uint32_t)v;
+    const uint32_t bmask = (1u << (w.sbits - 3)) - 1u;
+    uint32_t h = want ? slot_of(v, w.sbits - 3) : 0u;
+    uint32_t probes = 0;
+    bool pending = want, fresh = false;
+    while (__any_sync(kFull, pending)) {
+        int r = kBucketFull;
+        if (pending) r = scan_bucket(load_bucket(w.spill + 8 * h), mine, w.shift, w.epoch);
+        const bool ins = pending && r < 8;
+        const unsigned grp = __match_any_sync(kFull, ins ? 8u * h + (uint32_t)r : 0xffffffffu);
+        if (ins) {
+            if ((grp & lanemask_lt()) == 0) {
+                store_slot(w.spill + 8 * h + r, mine);
+                fresh = true;
+                pending = false;
+            }
+        } else if (pending) {
+            if (r < kBucketFull) {
+                pending = false;  // already visited
+            } else {
+                h = (h + 1u) & bmask;
+                if (++probes > bmask) {
+                    pending = false;
+                    bad = true;
+                }
             }
         }
-#pragma unroll
-        for (int t = 0; t < 8; ++t)
-            if (v[t] != -1) visit_global(w.spill, w.sbits, w.epoch, v[t]);
-        (void)mask;
+        __syncwarp();
     }
+    return fresh;
+}
+
+// Warp-collective visited check of one candidate per lane (`want`) in the query's current table.
+__device__ __forceinline__ bool visit_all(WarpState &w, bool want, int32_t v, bool &bad) {
+    if (w.epoch) return visit_global_warp(w, want, v, bad);
+    return want && visit_shared(w.tab, w.tbits, v);
+}
+
+// Gives the current query the next tag of the warp's global table; when the tags wrap, the
+// table is cleared first so that no slot carries a reused tag.
+__device__ __forceinline__ void spill_begin(WarpState &w, int lane) {
+    uint32_t c = 0;
+    if (lane == 0) c = atomicAdd(w.spill_epoch, 1u);
+    c = __shfl_sync(kFull, c, 0);
+    const uint32_t ntags = (1u << (32 - w.shift)) - 1u;
+    const uint32_t t = c % ntags;
+    if (t == 0) {
+        const int n = 1 << w.sbits;
+        for (int j = lane * 4; j < n; j += 128) *reinterpret_cast<uint4 *>(w.spill + j) = make_uint4(0, 0, 0, 0);
+        __syncwarp();
+    }
+    w.epoch = t + 1u;
+}
+
+// Moves the visited set from the shared-memory table into the warp's global table under a fresh
+// tag and continues there: the set is unchanged, only its storage grows.
+__device__ __forceinline__ void migrate_visited(WarpState &w, int lane, bool &bad) {
+    spill_begin(w, lane);
+    const int tsize = 1 << w.tbits;
+    for (int j0 = 0; j0 < tsize; j0 += 32) {
+        const int32_t v = w.tab[j0 + lane];
+        visit_global_warp(w, v != -1, v, bad);
+    }
+    __syncwarp();
+}
+
+// merge() for at most 32 surviving candidates (cand_{key,id}[0..ns), arrival order) and a pool of
+// at most 128 entries, in registers.  Candidate j (lane j): rank_j among the candidates, ub_j =
+// pool entries with key <= key_j, found from the last keys of the pool's 4-entry groups (one
+// ballot per candidate) and one 16-byte read of its group; slot_j = ub_j + rank_j.  Pool entry p
+// moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).  Everything that
+// moves is read first, then written once; whatever lands at cap or beyond is dropped.
+__device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &lb, int m, int ns, int lane) {
+    const bool has = lane < ns;
+    const uint32_t kj = has ? w.cand_key[lane] : 0xffffffffu;
+    const int32_t ij = has ? w.cand_id[lane] : 0;
+    const bool full = 4 * lane + 3 < S;
+    const uint32_t piv = full ? w.pkey[4 * lane + 3] : 0u;
+    int rank = 0, grp = 0;
+    for (int i = 0; i < ns; ++i) {
+        const uint32_t ki = __shfl_sync(kFull, kj, i);
+        const unsigned b = __ballot_sync(kFull, full && piv <= ki);
+        if (lane == i) grp = __popc(b);
+        rank += (ki < kj) || (ki == kj && i < lane);
+    }
+    int ub = 0x7fffffff;  // lanes without a candidate
+    if (has) {
+        // the group's four keys: 4*grp + 3 < capacity rounded up to 32, so the read stays in the pool
+        const int g0 = 4 * grp;
+        const uint4 gk = *reinterpret_cast<const uint4 *>(w.pkey + g0);
+        ub = g0 + (int)(g0 < S && gk.x <= kj) + (int)(g0 + 1 < S && gk.y <= kj) + (int)(g0 + 2 < S && gk.z <= kj) +
+             (int)(g0 + 3 < S && gk.w <= kj);
+    }
+    const int slot = has ? ub + rank : 0x7fffffff;
+    const bool acc = has && slot < cap;
+    // the rank-0 candidate always fits (its key is below the last entry of a full pool)
+    const int lo = (int)__reduce_min_sync(kFull, acc ? (unsigned)slot : 0x7fffffffu);
+    // pool entries in [lo, S) (S <= 128: at most four per lane) and how far each moves
+    uint32_t pk[4];
+    int32_t pi[4];
+    int pp[4], sh[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        pp[t] = lo + lane + 32 * t;
+        sh[t] = 0;
+        const bool in = pp[t] < S;
+        pk[t] = in ? w.pkey[pp[t]] : 0u;
+        pi[t] = in ? w.pid[pp[t]] : 0;
+    }
+    for (int i = 0; i < ns; ++i) {
+        const int ui = __shfl_sync(kFull, ub, i);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) sh[t] += ui <= pp[t];
+    }
+    const int sl = __popc(__ballot_sync(kFull, has && ub <= lb));
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int q = pp[t] + sh[t];
+        if (pp[t] < S && sh[t] > 0 && q < cap) {
+            w.pkey[q] = pk[t];
+            w.pid[q] = pi[t];
+        }
+    }
+    if (acc) {
+        w.pkey[slot] = kj;
+        w.pid[slot] = ij;
+    }
+    // new lower bound of the first unexpanded entry: the first candidate, or where the old bound
+    // moved to
+    const int nl = lb + sl;
+    lb = lo < nl ? lo : nl;
+    S = (S + m) < cap ? (S + m) : cap;
     __syncwarp();
 }
 
@@ -200,6 +326,10 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
         w.cand_id[t] = i1;
     }
     __syncwarp();
+    if (ns <= 32 && S <= 128) {
+        merge_small(w, S, cap, lb, m, ns, lane);
+        return;
+    }
     int nacc = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -398,7 +528,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         tlimit = (tsize >> 2) * 3;
     } else {
         spill_begin(w, lane);
-        tlimit = ((1 << w.sbits) >> 2) * 3;
+        tlimit = (1 << w.sbits) - ((1 << w.sbits) >> 3);
     }
 
     int S = 0, lb = 0, nvis = 0, cmps = 0, nexp = 0;
@@ -462,8 +592,10 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         __syncwarp();
         merge(w, S, cap, lb, 1, lane);
-        if (lane == 0) visit(w, u);
+        bool bad = false;
+        visit_all(w, lane == 0, u, bad);
         nvis += 1;
+        if (__any_sync(kFull, bad)) overflow = true;
         __syncwarp();
     } else {
         for (int e0 = 0; e0 < ix.nep; e0 += kMaxDegree) {
@@ -473,8 +605,13 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
             cmps += m;
             merge(w, S, cap, lb, m, lane);
-            for (int j = lane; j < m; j += 32) visit(w, w.cand_id[j]);
+            bool bad = false;
+            for (int j0 = 0; j0 < m; j0 += 32) {
+                const int j = j0 + lane;
+                visit_all(w, j < m, j < m ? w.cand_id[j] : 0, bad);
+            }
             nvis += m;
+            if (__any_sync(kFull, bad)) overflow = true;
             __syncwarp();
             if (nvis > tlimit) { overflow = true; break; }
         }
@@ -489,8 +626,10 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         if (f >= S || f >= lim) break;
         if (nvis + ix.K > tlimit) {
             if (w.spill && w.epoch == 0) {
-                migrate_visited(w, lane);
-                tlimit = ((1 << w.sbits) >> 2) * 3;
+                bool bad = false;
+                migrate_visited(w, lane, bad);
+                tlimit = (1 << w.sbits) - ((1 << w.sbits) >> 3);
+                if (__any_sync(kFull, bad)) { overflow = true; break; }
             }
             if (nvis + ix.K > tlimit) { overflow = true; break; }
         }
@@ -508,6 +647,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             r1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
         }
         int m = 0;
+        const bool staged = IsIntKind<KIND>::value && L.stage_row > 0;
         for (int c0 = 0; c0 < ix.K; c0 += 32) {
             const int v = c0 == 0 ? r0 : r1;
             const unsigned endm = __ballot_sync(kFull, v == -1);
@@ -516,15 +656,36 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             const unsigned same = __match_any_sync(kFull, v);
             const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
             const bool first = valid && ((same & vmask & lanemask_lt()) == 0);
-            if ((L.prefetch & kPrefetchNeighbours) && first) {
+            uint8_t *srow = nullptr;
+            if (staged) {
+                // copy the code row into shared memory now, so that it arrives during the visited check
+                srow = w.stage + lane * L.stage_row;
+                if (first) {
+                    const uint8_t *c = ix.codes + (size_t)v * (size_t)ix.csize;
+                    for (int o = 0; o < L.stage_row; o += 16) cp_async16(srow + o, c + o);
+                }
+                cp_async_commit();
+            } else if ((L.prefetch & kPrefetchNeighbours) && first) {
                 // start the code row's way into L1 now, so that it overlaps the visited check
                 const uint8_t *c = ix.codes + (size_t)v * (size_t)ix.csize;
                 asm volatile("prefetch.global.L1 [%0];" ::"l"(c));
                 if (ix.csize > 128) asm volatile("prefetch.global.L1 [%0];" ::"l"(c + 128));
             }
-            const bool fresh = first && visit(w, v);
+            bool bad = false;
+            const bool fresh = visit_all(w, first, v, bad);
+            if (__any_sync(kFull, bad)) overflow = true;
             const unsigned nm = __ballot_sync(kFull, fresh);
-            if (fresh) w.cand_id[m + __popc(nm & lanemask_lt())] = v;
+            const int at = m + __popc(nm & lanemask_lt());
+            if (staged) {
+                // distance of this lane's own neighbour from the staged row (one lane per row)
+                cp_async_wait_all();
+                if (fresh) {
+                    const int32_t part = sq_partial_row<KIND, METRIC>(reinterpret_cast<const uint4 *>(srow),
+                                                                      L.stage_row >> 4, w.qc);
+                    w.cand_key[at] = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
+                }
+            }
+            if (fresh) w.cand_id[at] = v;
             m += __popc(nm);
             if (endm) break;
         }
@@ -534,7 +695,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             pred_u = -1;
             continue;
         }
-        compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
+        if (!staged) compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
         cmps += m;
         // start the next row's load now, so that it arrives while the merge runs
         pred_u = (L.prefetch & kSpeculateRow) ? predict_next(w, S, cap, lb, lim, m, lane) : -1;
@@ -632,7 +793,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
 }
 
 template <int KIND, int METRIC, int LPR>
-__global__ void __launch_bounds__(256) search_kernel(IndexView ix, BatchView bv, WarpLayout L) {
+__global__ void __launch_bounds__(256, IsIntKind<KIND>::value ? 4 : 2) search_kernel(IndexView ix, BatchView bv, WarpLayout L) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -647,10 +808,12 @@ __global__ void __launch_bounds__(256) search_kernel(IndexView ix, BatchView bv,
     w.acc_id = reinterpret_cast<int32_t *>(ws + L.acc_id);
     w.fq = reinterpret_cast<float *>(ws + L.fq);
     w.qc = reinterpret_cast<uint32_t *>(ws + L.qc);
+    w.stage = ws + L.stage;
     const size_t slot = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     w.spill = bv.gtab ? bv.gtab + (slot << bv.gtab_bits) : nullptr;
     w.spill_epoch = bv.gtab ? bv.gtab_epoch + slot : nullptr;
     w.sbits = bv.gtab_bits;
+    w.shift = bv.gtab_shift;
     w.epoch = 0;
     w.shared_first = L.table_bits > 0;
     w.tab = reinterpret_cast<int32_t *>(ws + L.table);
@@ -819,6 +982,14 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     else if (ix.kind == K_SQ8U) off += up(ix.csize, 16);
     L->table = off;
     if (table_bits > 0) off += (1 << table_bits) * 4;
+    off = up(off, 16);
+    L->stage = off;
+    L->stage_row = 0;
+    if ((ix.kind == K_SQ4U || ix.kind == K_SQ8U) && !(prefetch & kNoStageCodes) && ix.csize <= 128 &&
+        ix.csize % 16 == 0) {
+        L->stage_row = ix.csize;
+        off += 32 * ix.csize;
+    }
     L->total = up(off, 16);
     L->cap = capa - 1;
     L->table_bits = table_bits;
