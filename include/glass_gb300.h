@@ -146,9 +146,9 @@ typedef struct {
     int32_t prefetch;         /* bit 3: do not stage neighbour code rows in shared memory during
                                  the visited check (staging applies to SQ8U/SQ4U rows of at most
                                  128 bytes); bit 2: prefetch each neighbour's code row into L1
-                                 before its visited check (unstaged rows); bit 1: no effect
-                                 (the next adjacency row is always loaded during the merge);
-                                 bit 0: also prefetch that row's code rows into L1 */
+                                 before its visited check (unstaged rows); bit 1: load the
+                                 predicted next adjacency row during the merge; bit 0: also
+                                 prefetch that row's code rows */
     int32_t spill_bits;       /* log2 of the slots of each warp's global visited table (4 bytes a
                                  slot; 7..20, 0 = sized from the visit counts seen) */
 } gsx_tuning;

@@ -15,9 +15,8 @@ constexpr int kMaxDegree = 64;       // graph degree handled per row (two 32-wid
 constexpr int kMaxCap = 1024;        // largest pool capacity max(k*factor, ef)
 constexpr int kMinTableBits = 7;     // smallest visited table: 128 slots
 constexpr int kGlobalOnly = 1;       // table_bits value: no shared table, visited set in global memory
-constexpr int kPrefetchCodes = 1;    // tuning.prefetch bit: L1 prefetch of the next row's codes
-                                     // (bit 2 is accepted and has no effect: the next row is always
-                                     // loaded during the merge)
+constexpr int kPrefetchCodes = 1;    // tuning.prefetch bit: L1 prefetch of the predicted row's codes
+constexpr int kSpeculateRow = 2;     // tuning.prefetch bit: load the predicted next row during the merge
 constexpr int kPrefetchNeighbours = 4;  // tuning.prefetch bit: L1 prefetch of each neighbour's codes
                                         // before its visited check
 constexpr int kNoStageCodes = 8;     // tuning.prefetch bit: do not stage neighbour code rows in shared

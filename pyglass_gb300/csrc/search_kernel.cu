@@ -439,6 +439,37 @@ __device__ __forceinline__ void refine_dists(const IndexView &ix, const int32_t 
     __syncwarp();
 }
 
+// The node the next expansion will pop, known before the merge: the first unexpanded pool entry,
+// unless the best candidate that can enter has a strictly smaller key (equal keys go after the
+// pool entry).  Used only to start loading that node's adjacency row early; the pop checks it.
+__device__ __forceinline__ int predict_next(const WarpState &w, int S, int cap, int lb, int lim, int m, int lane) {
+    const int hi = S < lim ? S : lim;
+    const int f0 = first_unchecked(w.pid, lb, hi, lane);
+    const bool has_pool = f0 < hi;
+    const uint32_t kf = has_pool ? w.pkey[f0] : 0xffffffffu;
+    const uint32_t last = S == cap ? w.pkey[S - 1] : 0xffffffffu;
+    uint32_t bk = 0xffffffffu;
+    int bj = kMaxDegree;
+    for (int j = lane; j < m; j += 32) {
+        const uint32_t k = w.cand_key[j];
+        if ((S < cap || k < last) && (k < bk || (k == bk && j < bj))) {
+            bk = k;
+            bj = j;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t ok = __shfl_xor_sync(kFull, bk, o);
+        const int oj = __shfl_xor_sync(kFull, bj, o);
+        if (ok < bk || (ok == bk && oj < bj)) {
+            bk = ok;
+            bj = oj;
+        }
+    }
+    if (bj < kMaxDegree && (!has_pool || bk < kf)) return w.cand_id[bj];
+    return has_pool ? (w.pid[f0] & kIdMask) : -1;
+}
+
 // Encodes the query held in w.fq into w.qc (SQ kinds); returns the sum of squared codes.
 template <int KIND, int METRIC>
 __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState &w, int lane) {
@@ -588,15 +619,11 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
 
     // ---- SearchImpl2 (graph_searcher.hpp:196-224) ----
     const int lim = ef_expand < cap ? ef_expand : cap;
-    int pred_u = -1;             // node whose adjacency row is already loaded (during the last merge)
+    int pred_u = -1;             // node whose row was loaded speculatively during the last merge
     int32_t pv0 = -1, pv1 = -1;  // that row: entries lane and 32 + lane
-    // f = the first unexpanded pool entry and fu its node; from here on both are carried exactly
-    // from one expansion to the next instead of being searched for
-    int f = first_unchecked(w.pid, lb, S < lim ? S : lim, lane);
-    int fu = f < (S < lim ? S : lim) ? (w.pid[f] & kIdMask) : -1;
     while (!overflow) {
-        const int hi = S < lim ? S : lim;
-        if (f >= hi) break;
+        const int f = first_unchecked(w.pid, lb, S < lim ? S : lim, lane);
+        if (f >= S || f >= lim) break;
         if (nvis + ix.K > tlimit) {
             if (w.spill && w.epoch == 0) {
                 bool bad = false;
@@ -606,8 +633,11 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             }
             if (nvis + ix.K > tlimit) { overflow = true; break; }
         }
-        const int u = fu;
-        if (lane == 0) w.pid[f] = u | kChecked;
+        const int32_t raw = w.pid[f];
+        __syncwarp();
+        if (lane == 0) w.pid[f] = raw | kChecked;
+        const int u = raw & kIdMask;
+        lb = f + 1;
         ++nexp;
         // adjacency row, stop at the first -1; skip repeats within the row and visited ids
         int32_t r0 = pv0, r1 = pv1;
@@ -616,12 +646,6 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             r0 = lane < ix.K ? __ldg(row + lane) : -1;
             r1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
         }
-        // the next unexpanded entry after f in the pool as it stands (overlaps the row load); the
-        // merge below moves it to its new place
-        const int f2 = first_unchecked(w.pid, f + 1, hi, lane);
-        const bool has2 = f2 < hi;
-        const uint32_t k2 = has2 ? w.pkey[f2] : 0xffffffffu;
-        const int32_t u2 = has2 ? (w.pid[f2] & kIdMask) : -1;
         int m = 0;
         const bool staged = IsIntKind<KIND>::value && L.stage_row > 0;
         for (int c0 = 0; c0 < ix.K; c0 += 32) {
@@ -668,34 +692,19 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         __syncwarp();
         nvis += m;
         if (m == 0) {
-            f = f2;
-            fu = u2;
             pred_u = -1;
             continue;
         }
         if (!staged) compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
         cmps += m;
-        // The next expansion pops the best new candidate (smallest key, earliest arrival) unless
-        // entry f2 has an equal or smaller key (a candidate goes after equal keys).  Its row is
-        // loaded now, so that it arrives while the merge runs.
-        {
-            const uint32_t c0k = lane < m ? w.cand_key[lane] : 0xffffffffu;
-            const uint32_t c1k = lane + 32 < m ? w.cand_key[lane + 32] : 0xffffffffu;
-            const uint32_t kmin = __reduce_min_sync(kFull, c0k < c1k ? c0k : c1k);
-            const unsigned b0 = __ballot_sync(kFull, lane < m && c0k == kmin);
-            const unsigned b1 = __ballot_sync(kFull, lane + 32 < m && c1k == kmin);
-            const int jmin = b0 ? __ffs(b0) - 1 : 31 + __ffs(b1);
-            fu = (has2 && k2 <= kmin) ? u2 : w.cand_id[jmin];
-            pred_u = fu;
-            const int32_t *row = ix.adj + (size_t)fu * (size_t)ix.K;
+        // start the next row's load now, so that it arrives while the merge runs
+        pred_u = (L.prefetch & kSpeculateRow) ? predict_next(w, S, cap, lb, lim, m, lane) : -1;
+        if (pred_u >= 0) {
+            const int32_t *row = ix.adj + (size_t)pred_u * (size_t)ix.K;
             pv0 = lane < ix.K ? __ldg(row + lane) : -1;
             pv1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
         }
-        // with lb = f2 the merge leaves lb at the exact new index of the first unexpanded entry:
-        // the first accepted candidate or f2's new place
-        lb = f2;
         merge(w, S, cap, lb, m, lane);
-        f = lb;
         if ((L.prefetch & kPrefetchCodes) && pred_u >= 0) {
             // the predicted row has arrived during the merge: pull its neighbours' code rows
             // towards L1 for the next expansion (a wrong prediction only wastes the prefetch;
