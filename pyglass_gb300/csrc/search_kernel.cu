@@ -216,20 +216,20 @@ __device__ __forceinline__ void migrate_visited(WarpState &w, int lane, bool &ba
     __syncwarp();
 }
 
-// merge() for at most 32 surviving candidates (cand_{key,id}[0..ns), arrival order) and a pool of
-// at most 128 entries, in registers.  Candidate j (lane j): rank_j among the candidates, ub_j =
-// pool entries with key <= key_j, found from the last keys of the pool's 4-entry groups (one
-// ballot per candidate) and one 16-byte read of its group; slot_j = ub_j + rank_j.  Pool entry p
-// moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).  Everything that
-// moves is read first, then written once; whatever lands at cap or beyond is dropped.
-__device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &lb, int m, int ns, int lane) {
-    const bool has = lane < ns;
-    const uint32_t kj = has ? w.cand_key[lane] : 0xffffffffu;
-    const int32_t ij = has ? w.cand_id[lane] : 0;
+// merge() for a pool of at most 128 entries with the surviving candidates held in registers: lane
+// j holds one when bit j of `sm` is set (has), lanes in arrival order.  Candidate j: rank_j among
+// the candidates, ub_j = pool entries with key <= key_j, found from the last keys of the pool's
+// 4-entry groups (one ballot per candidate) and one 16-byte read of its group; slot_j = ub_j +
+// rank_j.  Pool entry p moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).
+// Everything that moves is read first, then written once; whatever lands at cap or beyond is
+// dropped.  m = all new candidates (survivors or not), for the pool size.
+__device__ __forceinline__ void merge_regs(WarpState &w, int &S, int cap, int &lb, int m, bool has, uint32_t kj,
+                                           int32_t ij, unsigned sm, int lane) {
     const bool full = 4 * lane + 3 < S;
     const uint32_t piv = full ? w.pkey[4 * lane + 3] : 0u;
     int rank = 0, grp = 0;
-    for (int i = 0; i < ns; ++i) {
+    for (unsigned it = sm; it; it &= it - 1) {
+        const int i = __ffs(it) - 1;
         const uint32_t ki = __shfl_sync(kFull, kj, i);
         const unsigned b = __ballot_sync(kFull, full && piv <= ki);
         if (lane == i) grp = __popc(b);
@@ -259,8 +259,8 @@ __device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &
         pk[t] = in ? w.pkey[pp[t]] : 0u;
         pi[t] = in ? w.pid[pp[t]] : 0;
     }
-    for (int i = 0; i < ns; ++i) {
-        const int ui = __shfl_sync(kFull, ub, i);
+    for (unsigned it = sm; it; it &= it - 1) {
+        const int ui = __shfl_sync(kFull, ub, __ffs(it) - 1);
 #pragma unroll
         for (int t = 0; t < 4; ++t) sh[t] += ui <= pp[t];
     }
@@ -284,6 +284,21 @@ __device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &
     lb = lo < nl ? lo : nl;
     S = (S + m) < cap ? (S + m) : cap;
     __syncwarp();
+}
+
+// merge() of new candidates held one per lane in arrival order (fresh lanes of a row of at most 32
+// neighbours), pool of at most 128 entries: the survivor filter of merge() then merge_regs, with no
+// trip through the candidate arrays.
+__device__ __forceinline__ void merge_lanes(WarpState &w, int &S, int cap, int &lb, int m, bool fresh, uint32_t kj,
+                                            int32_t ij, int lane) {
+    const uint32_t last = S == cap ? w.pkey[S - 1] : 0xffffffffu;
+    const bool has = fresh && (S < cap || kj < last);
+    const unsigned sm = __ballot_sync(kFull, has);
+    if (sm == 0) {
+        S = (S + m) < cap ? (S + m) : cap;
+        return;
+    }
+    merge_regs(w, S, cap, lb, m, has, has ? kj : 0xffffffffu, ij, sm, lane);
 }
 
 // Merges candidates cand_{id,key}[0..m) (in insertion order, m <= 64) into the pool
@@ -327,7 +342,9 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     }
     __syncwarp();
     if (ns <= 32 && S <= 128) {
-        merge_small(w, S, cap, lb, m, ns, lane);
+        const bool has = lane < ns;
+        merge_regs(w, S, cap, lb, m, has, has ? w.cand_key[lane] : 0xffffffffu, has ? w.cand_id[lane] : 0,
+                   ns == 32 ? kFull : (1u << ns) - 1u, lane);
         return;
     }
     int nacc = 0;
@@ -485,6 +502,7 @@ __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState 
             uint32_t lo = word & 0x0F0F0F0Fu, hi = (word >> 4) & 0x0F0F0F0Fu;
             w.qc[wi] = lo;
             w.qc[nw + wi] = hi;
+            w.qc[2 * nw + wi] = lo << 4;  // low nibbles x16, for sq_cross2_row
             sq = __dp4a(lo, lo, (uint32_t)sq);
             sq = __dp4a(hi, hi, (uint32_t)sq);
         } else {
@@ -619,6 +637,10 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
 
     // ---- SearchImpl2 (graph_searcher.hpp:196-224) ----
     const int lim = ef_expand < cap ? ef_expand : cap;
+    // staged rows of at most 32 neighbours and a pool of at most 128: the new candidates stay in
+    // registers, one per lane, from the visited check to the merge
+    const bool fused = IsIntKind<KIND>::value && L.stage_row > 0 && ix.K <= 32 && cap <= 128 &&
+                       !(L.prefetch & kSpeculateRow);
     int pred_u = -1;             // node whose row was loaded speculatively during the last merge
     int32_t pv0 = -1, pv1 = -1;  // that row: entries lane and 32 + lane
     while (!overflow) {
@@ -648,6 +670,9 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         int m = 0;
         const bool staged = IsIntKind<KIND>::value && L.stage_row > 0;
+        bool lf = false;       // fused: this lane's neighbour is new
+        uint32_t lkey = 0;     // fused: its key
+        int32_t lv = 0;        // fused: its id
         for (int c0 = 0; c0 < ix.K; c0 += 32) {
             const int v = c0 == 0 ? r0 : r1;
             const unsigned endm = __ballot_sync(kFull, v == -1);
@@ -657,12 +682,14 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
             const bool first = valid && ((same & vmask & lanemask_lt()) == 0);
             uint8_t *srow = nullptr;
+            int32_t xn = 0;
             if (staged) {
                 // copy the code row into shared memory now, so that it arrives during the visited check
                 srow = w.stage + lane * L.stage_row;
                 if (first) {
                     const uint8_t *c = ix.codes + (size_t)v * (size_t)ix.csize;
                     for (int o = 0; o < L.stage_row; o += 16) cp_async16(srow + o, c + o);
+                    if (ix.norms) xn = __ldg(ix.norms + v);
                 }
                 cp_async_commit();
             } else if ((L.prefetch & kPrefetchNeighbours) && first) {
@@ -680,12 +707,20 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
                 // distance of this lane's own neighbour from the staged row (one lane per row)
                 cp_async_wait_all();
                 if (fresh) {
-                    const int32_t part = sq_partial_row<KIND, METRIC>(reinterpret_cast<const uint4 *>(srow),
-                                                                      L.stage_row >> 4, w.qc);
-                    w.cand_key[at] = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
+                    const uint4 *sr = reinterpret_cast<const uint4 *>(srow);
+                    const int32_t part = ix.norms ? xn - sq_cross2_row<KIND>(sr, L.stage_row >> 4, w.qc)
+                                                  : sq_partial_row<KIND, METRIC>(sr, L.stage_row >> 4, w.qc);
+                    const uint32_t key = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
+                    if (fused) lkey = key;
+                    else w.cand_key[at] = key;
                 }
             }
-            if (fresh) w.cand_id[at] = v;
+            if (fused) {
+                lf = fresh;
+                lv = v;
+            } else if (fresh) {
+                w.cand_id[at] = v;
+            }
             m += __popc(nm);
             if (endm) break;
         }
@@ -697,6 +732,10 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         if (!staged) compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
         cmps += m;
+        if (fused) {
+            merge_lanes(w, S, cap, lb, m, lf, lkey, lv, lane);
+            continue;
+        }
         // start the next row's load now, so that it arrives while the merge runs
         pred_u = (L.prefetch & kSpeculateRow) ? predict_next(w, S, cap, lb, lim, m, lane) : -1;
         if (pred_u >= 0) {
@@ -978,7 +1017,7 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     L->fq = off; off += fq * 4;
     L->fq_len = fq;
     L->qc = off;
-    if (ix.kind == K_SQ4U) off += up(2 * ix.csize, 16);
+    if (ix.kind == K_SQ4U) off += up(3 * ix.csize, 16);
     else if (ix.kind == K_SQ8U) off += up(ix.csize, 16);
     L->table = off;
     if (table_bits > 0) off += (1 << table_bits) * 4;
