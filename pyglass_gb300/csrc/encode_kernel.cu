@@ -45,28 +45,6 @@ __global__ void pad_rows(const float *__restrict__ data, int64_t n, int d, int d
     }
 }
 
-// Squared norm of each code row (sum of the squared 4-bit or 8-bit codes): the query-independent
-// term of the L2 code distance, so the search only forms the cross term.
-template <int KIND>
-__global__ void row_norms(const uint32_t *__restrict__ codes, int64_t n, int csize, int32_t *__restrict__ out) {
-    const int nw = csize >> 2;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t *row = codes + r * nw;
-        uint32_t s = 0;
-        for (int i = 0; i < nw; ++i) {
-            const uint32_t x = row[i];
-            if (KIND == K_SQ4U) {
-                const uint32_t lo = x & 0x0F0F0F0Fu, hi = (x >> 4) & 0x0F0F0F0Fu;
-                s = __dp4a(lo, lo, s);
-                s = __dp4a(hi, hi, s);
-            } else {
-                s = __dp4a(x, x, s);
-            }
-        }
-        out[r] = (int32_t)s;
-    }
-}
-
 int grid_for(int64_t work) {
     int64_t g = (work + 255) / 256;
     if (g > 152 * 32) g = 152 * 32;
@@ -85,14 +63,6 @@ cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, in
     else if (kind == K_SQ8U && metric == M_IP) encode_rows<K_SQ8U, M_IP><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
     else if (kind == K_SQ8U) encode_rows<K_SQ8U, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
     else if (kind == K_E5M2) encode_rows<K_E5M2, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
-    else return cudaErrorInvalidValue;
-    return cudaGetLastError();
-}
-
-cudaError_t launch_row_norms(int kind, const uint8_t *codes, int64_t n, int csize, int32_t *out, cudaStream_t st) {
-    const uint32_t *c = reinterpret_cast<const uint32_t *>(codes);
-    if (kind == K_SQ4U) row_norms<K_SQ4U><<<grid_for(n), 256, 0, st>>>(c, n, csize, out);
-    else if (kind == K_SQ8U) row_norms<K_SQ8U><<<grid_for(n), 256, 0, st>>>(c, n, csize, out);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }

@@ -563,7 +563,7 @@ void gsx_searcher_destroy(gsx_searcher *s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
-    for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->norms, &s->q, &s->ids,
+    for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->q, &s->ids,
                       &s->dis, &s->status, &s->cmps, &s->efp, &s->kp, &s->order, &s->counters, &s->gtab.buf,
                       &s->spill.buf, &s->dist_out, &s->dist_ids})
         b->release();
@@ -596,12 +596,6 @@ int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t
         GSX_CUDA(launch_encode(s->kind, s->metric, raw.as<float>(), n, dim, ix.dalign, ix.csize, ix.p0, ix.p1,
                                s->codes.as<uint8_t>(), st));
     }
-    // squared code norms for the L2 code distances (the search then forms only the cross term)
-    const bool want_norms = s->kind == K_SQ4U || (s->kind == K_SQ8U && s->metric == M_L2);
-    if (want_norms) {
-        if ((rc = s->norms.ensure((size_t)n * 4))) return rc;
-        GSX_CUDA(launch_row_norms(s->kind, s->codes.as<uint8_t>(), n, ix.csize, s->norms.as<int32_t>(), st));
-    }
     if (s->has_refine) {
         ix.r_dalign = (dim + 15) / 16 * 16;
         if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 4))) return rc;
@@ -610,7 +604,6 @@ int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t
     GSX_CUDA(cudaStreamSynchronize(st));
     ix.codes = s->codes.as<uint8_t>();
     ix.r_codes = s->r_codes.as<float>();
-    ix.norms = want_norms ? s->norms.as<int32_t>() : nullptr;
     // keep 1,000 sampled rows for optimize (graph_searcher.hpp:62-69)
     s->sample_n = std::min(1000, n);
     std::mt19937 rng(12345);
@@ -768,7 +761,7 @@ int gsx_searcher_memory(const gsx_searcher *s, size_t *index_bytes, size_t *per_
     if (!s) return fail(GSX_ERR_INVALID, "null searcher");
     if (index_bytes)
         *index_bytes = s->adj.bytes + s->eps.bytes + s->levels.bytes + s->loff.bytes + s->lists.bytes + s->codes.bytes +
-                       s->r_codes.bytes + s->norms.bytes;
+                       s->r_codes.bytes;
     if (per_query_bytes) {
         // device bytes one in-flight query holds outside the resident index: its fp32 row,
         // outputs (k up to 256), status and counter

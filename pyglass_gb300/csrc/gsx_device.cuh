@@ -194,41 +194,6 @@ __device__ __forceinline__ int32_t sq_partial_row(const uint4 *row, int nch, con
     }
 }
 
-// Twice the cross term 2*sum(x*q) of an L2 code distance over a whole row in shared memory (one
-// lane per row), for use with a precomputed row norm: |x-q|^2 = |q|^2 + |x|^2 - 2*sum(x*q), all
-// exact integers.  SQ4U reads the query's low nibbles pre-scaled by 16 (qc + 8*nch) and masks the
-// high nibbles in place, so each 32-bit word takes two dp4a and the sum comes out as 16*sum(x*q).
-template <int KIND>
-__device__ __forceinline__ int32_t sq_cross2_row(const uint4 *row, int nch, const uint32_t *qc) {
-    uint32_t acc = 0;
-    if (KIND == K_SQ4U) {
-        const uint4 *qh = reinterpret_cast<const uint4 *>(qc + 4 * nch);
-        const uint4 *ql16 = reinterpret_cast<const uint4 *>(qc + 8 * nch);
-#pragma unroll 4
-        for (int c = 0; c < nch; ++c) {
-            const uint4 v = row[c];
-            const uint4 l = ql16[c], h = qh[c];
-            acc = __dp4a(v.x & 0x0F0F0F0Fu, l.x, acc); acc = __dp4a(v.x & 0xF0F0F0F0u, h.x, acc);
-            acc = __dp4a(v.y & 0x0F0F0F0Fu, l.y, acc); acc = __dp4a(v.y & 0xF0F0F0F0u, h.y, acc);
-            acc = __dp4a(v.z & 0x0F0F0F0Fu, l.z, acc); acc = __dp4a(v.z & 0xF0F0F0F0u, h.z, acc);
-            acc = __dp4a(v.w & 0x0F0F0F0Fu, l.w, acc); acc = __dp4a(v.w & 0xF0F0F0F0u, h.w, acc);
-        }
-        return (int32_t)(acc >> 3);
-    } else {
-        const uint4 *qv = reinterpret_cast<const uint4 *>(qc);
-#pragma unroll 4
-        for (int c = 0; c < nch; ++c) {
-            const uint4 v = row[c];
-            const uint4 q = qv[c];
-            acc = __dp4a(v.x, q.x, acc);
-            acc = __dp4a(v.y, q.y, acc);
-            acc = __dp4a(v.z, q.z, acc);
-            acc = __dp4a(v.w, q.w, acc);
-        }
-        return 2 * (int32_t)acc;
-    }
-}
-
 // Finishes a team's integer distance (all lanes of the warp must call it).
 template <int KIND, int METRIC, int LPR>
 __device__ __forceinline__ int32_t sq_finish(int32_t partial, int32_t qsq) {

@@ -81,7 +81,7 @@ struct gsx_searcher {
     // device index
     bool has_data = false;
     gsx::IndexView ix{};
-    gsx::DevBuf adj, eps, levels, loff, lists, codes, r_codes, norms;
+    gsx::DevBuf adj, eps, levels, loff, lists, codes, r_codes;
     cudaStream_t stream = nullptr;
     int num_sms = 0;
 

@@ -39,7 +39,6 @@ struct IndexView {
     float refine_factor;
     int32_t r_dalign;
     const float *r_codes;     // N*r_dalign fp32 rows
-    const int32_t *norms;     // N squared norms of the code rows (SQ4U, SQ8U L2), or null
 };
 
 // One batched launch.
@@ -105,7 +104,6 @@ int search_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg);
 cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, int d, int dalign, int csize, float p0,
                           float p1, uint8_t *out, cudaStream_t st);
 cudaError_t launch_pad_rows(const float *data, int64_t n, int d, int dalign, float *out, cudaStream_t st);
-cudaError_t launch_row_norms(int kind, const uint8_t *codes, int64_t n, int csize, int32_t *out, cudaStream_t st);
 cudaError_t launch_distances(const IndexView &ix, int refine, const float *queries, int nq, const int32_t *ids,
                              int m, double *out, cudaStream_t st);
 

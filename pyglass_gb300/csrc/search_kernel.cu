@@ -502,7 +502,6 @@ __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState 
             uint32_t lo = word & 0x0F0F0F0Fu, hi = (word >> 4) & 0x0F0F0F0Fu;
             w.qc[wi] = lo;
             w.qc[nw + wi] = hi;
-            w.qc[2 * nw + wi] = lo << 4;  // low nibbles x16, for sq_cross2_row
             sq = __dp4a(lo, lo, (uint32_t)sq);
             sq = __dp4a(hi, hi, (uint32_t)sq);
         } else {
@@ -682,14 +681,12 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
             const bool first = valid && ((same & vmask & lanemask_lt()) == 0);
             uint8_t *srow = nullptr;
-            int32_t xn = 0;
             if (staged) {
                 // copy the code row into shared memory now, so that it arrives during the visited check
                 srow = w.stage + lane * L.stage_row;
                 if (first) {
                     const uint8_t *c = ix.codes + (size_t)v * (size_t)ix.csize;
                     for (int o = 0; o < L.stage_row; o += 16) cp_async16(srow + o, c + o);
-                    if (ix.norms) xn = __ldg(ix.norms + v);
                 }
                 cp_async_commit();
             } else if ((L.prefetch & kPrefetchNeighbours) && first) {
@@ -707,9 +704,8 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
                 // distance of this lane's own neighbour from the staged row (one lane per row)
                 cp_async_wait_all();
                 if (fresh) {
-                    const uint4 *sr = reinterpret_cast<const uint4 *>(srow);
-                    const int32_t part = ix.norms ? xn - sq_cross2_row<KIND>(sr, L.stage_row >> 4, w.qc)
-                                                  : sq_partial_row<KIND, METRIC>(sr, L.stage_row >> 4, w.qc);
+                    const int32_t part = sq_partial_row<KIND, METRIC>(reinterpret_cast<const uint4 *>(srow),
+                                                                      L.stage_row >> 4, w.qc);
                     const uint32_t key = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
                     if (fused) lkey = key;
                     else w.cand_key[at] = key;
@@ -1017,7 +1013,7 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     L->fq = off; off += fq * 4;
     L->fq_len = fq;
     L->qc = off;
-    if (ix.kind == K_SQ4U) off += up(3 * ix.csize, 16);
+    if (ix.kind == K_SQ4U) off += up(2 * ix.csize, 16);
     else if (ix.kind == K_SQ8U) off += up(ix.csize, 16);
     L->table = off;
     if (table_bits > 0) off += (1 << table_bits) * 4;
