@@ -216,20 +216,20 @@ __device__ __forceinline__ void migrate_visited(WarpState &w, int lane, bool &ba
     __syncwarp();
 }
 
-// merge() for a pool of at most 128 entries with the surviving candidates held in registers: lane
-// j holds one when bit j of `sm` is set (has), lanes in arrival order.  Candidate j: rank_j among
-// the candidates, ub_j = pool entries with key <= key_j, found from the last keys of the pool's
-// 4-entry groups (one ballot per candidate) and one 16-byte read of its group; slot_j = ub_j +
-// rank_j.  Pool entry p moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).
-// Everything that moves is read first, then written once; whatever lands at cap or beyond is
-// dropped.  m = all new candidates (survivors or not), for the pool size.
-__device__ __forceinline__ void merge_regs(WarpState &w, int &S, int cap, int &lb, int m, bool has, uint32_t kj,
-                                           int32_t ij, unsigned sm, int lane) {
+// merge() for at most 32 surviving candidates (cand_{key,id}[0..ns), arrival order) and a pool of
+// at most 128 entries, in registers.  Candidate j (lane j): rank_j among the candidates, ub_j =
+// pool entries with key <= key_j, found from the last keys of the pool's 4-entry groups (one
+// ballot per candidate) and one 16-byte read of its group; slot_j = ub_j + rank_j.  Pool entry p
+// moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).  Everything that
+// moves is read first, then written once; whatever lands at cap or beyond is dropped.
+__device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &lb, int m, int ns, int lane) {
+    const bool has = lane < ns;
+    const uint32_t kj = has ? w.cand_key[lane] : 0xffffffffu;
+    const int32_t ij = has ? w.cand_id[lane] : 0;
     const bool full = 4 * lane + 3 < S;
     const uint32_t piv = full ? w.pkey[4 * lane + 3] : 0u;
     int rank = 0, grp = 0;
-    for (unsigned it = sm; it; it &= it - 1) {
-        const int i = __ffs(it) - 1;
+    for (int i = 0; i < ns; ++i) {
         const uint32_t ki = __shfl_sync(kFull, kj, i);
         const unsigned b = __ballot_sync(kFull, full && piv <= ki);
         if (lane == i) grp = __popc(b);
@@ -259,8 +259,8 @@ __device__ __forceinline__ void merge_regs(WarpState &w, int &S, int cap, int &l
         pk[t] = in ? w.pkey[pp[t]] : 0u;
         pi[t] = in ? w.pid[pp[t]] : 0;
     }
-    for (unsigned it = sm; it; it &= it - 1) {
-        const int ui = __shfl_sync(kFull, ub, __ffs(it) - 1);
+    for (int i = 0; i < ns; ++i) {
+        const int ui = __shfl_sync(kFull, ub, i);
 #pragma unroll
         for (int t = 0; t < 4; ++t) sh[t] += ui <= pp[t];
     }
@@ -284,21 +284,6 @@ __device__ __forceinline__ void merge_regs(WarpState &w, int &S, int cap, int &l
     lb = lo < nl ? lo : nl;
     S = (S + m) < cap ? (S + m) : cap;
     __syncwarp();
-}
-
-// merge() of new candidates held one per lane in arrival order (fresh lanes of a row of at most 32
-// neighbours), pool of at most 128 entries: the survivor filter of merge() then merge_regs, with no
-// trip through the candidate arrays.
-__device__ __forceinline__ void merge_lanes(WarpState &w, int &S, int cap, int &lb, int m, bool fresh, uint32_t kj,
-                                            int32_t ij, int lane) {
-    const uint32_t last = S == cap ? w.pkey[S - 1] : 0xffffffffu;
-    const bool has = fresh && (S < cap || kj < last);
-    const unsigned sm = __ballot_sync(kFull, has);
-    if (sm == 0) {
-        S = (S + m) < cap ? (S + m) : cap;
-        return;
-    }
-    merge_regs(w, S, cap, lb, m, has, has ? kj : 0xffffffffu, ij, sm, lane);
 }
 
 // Merges candidates cand_{id,key}[0..m) (in insertion order, m <= 64) into the pool
@@ -342,9 +327,7 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     }
     __syncwarp();
     if (ns <= 32 && S <= 128) {
-        const bool has = lane < ns;
-        merge_regs(w, S, cap, lb, m, has, has ? w.cand_key[lane] : 0xffffffffu, has ? w.cand_id[lane] : 0,
-                   ns == 32 ? kFull : (1u << ns) - 1u, lane);
+        merge_small(w, S, cap, lb, m, ns, lane);
         return;
     }
     int nacc = 0;
@@ -636,10 +619,6 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
 
     // ---- SearchImpl2 (graph_searcher.hpp:196-224) ----
     const int lim = ef_expand < cap ? ef_expand : cap;
-    // staged rows of at most 32 neighbours and a pool of at most 128: the new candidates stay in
-    // registers, one per lane, from the visited check to the merge
-    const bool fused = IsIntKind<KIND>::value && L.stage_row > 0 && ix.K <= 32 && cap <= 128 &&
-                       !(L.prefetch & kSpeculateRow);
     int pred_u = -1;             // node whose row was loaded speculatively during the last merge
     int32_t pv0 = -1, pv1 = -1;  // that row: entries lane and 32 + lane
     while (!overflow) {
@@ -669,9 +648,6 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         int m = 0;
         const bool staged = IsIntKind<KIND>::value && L.stage_row > 0;
-        bool lf = false;       // fused: this lane's neighbour is new
-        uint32_t lkey = 0;     // fused: its key
-        int32_t lv = 0;        // fused: its id
         for (int c0 = 0; c0 < ix.K; c0 += 32) {
             const int v = c0 == 0 ? r0 : r1;
             const unsigned endm = __ballot_sync(kFull, v == -1);
@@ -706,17 +682,10 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
                 if (fresh) {
                     const int32_t part = sq_partial_row<KIND, METRIC>(reinterpret_cast<const uint4 *>(srow),
                                                                       L.stage_row >> 4, w.qc);
-                    const uint32_t key = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
-                    if (fused) lkey = key;
-                    else w.cand_key[at] = key;
+                    w.cand_key[at] = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
                 }
             }
-            if (fused) {
-                lf = fresh;
-                lv = v;
-            } else if (fresh) {
-                w.cand_id[at] = v;
-            }
+            if (fresh) w.cand_id[at] = v;
             m += __popc(nm);
             if (endm) break;
         }
@@ -728,10 +697,6 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         if (!staged) compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
         cmps += m;
-        if (fused) {
-            merge_lanes(w, S, cap, lb, m, lf, lkey, lv, lane);
-            continue;
-        }
         // start the next row's load now, so that it arrives while the merge runs
         pred_u = (L.prefetch & kSpeculateRow) ? predict_next(w, S, cap, lb, lim, m, lane) : -1;
         if (pred_u >= 0) {
