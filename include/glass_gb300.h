@@ -143,7 +143,9 @@ typedef struct {
     int32_t table_bits;       /* log2 of the per-query visited-table slots in shared memory
                                  (1 = none: the visited set lives in the warp's global table) */
     int32_t lanes_per_row;    /* lanes cooperating on one code row (SQ kinds) */
-    int32_t prefetch;         /* bit 3: do not stage neighbour code rows in shared memory during
+    int32_t prefetch;         /* bit 4: run batches larger than one wave of resident warps in index
+                                 order instead of sorted along the base data's principal
+                                 direction (the order never changes a result); bit 3: do not stage neighbour code rows in shared memory during
                                  the visited check (staging applies to SQ8U/SQ4U rows of at most
                                  128 bytes); bit 2: prefetch each neighbour's code row into L1
                                  before its visited check (unstaged rows); bit 1: load the

@@ -209,6 +209,51 @@ int spill_bits_for(const gsx_searcher *s, const LaunchCfg &cfg) {
     return bits + 1;
 }
 
+// Direction of the batch order: the principal direction of the sampled base rows (power iteration
+// from the all-ones vector, 30 steps, in double), their mean, and the bin scale that spreads the
+// sample's projections over the order's bins with 10% margin on each side.
+int batch_order_setup(gsx_searcher *s) {
+    const int n = s->sample_n, d = s->ix.d;
+    std::vector<double> mean(d, 0.0), v(d, 1.0 / std::sqrt((double)d)), w(d);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < d; ++j) mean[j] += s->sample[(size_t)i * d + j];
+    for (int j = 0; j < d; ++j) mean[j] /= n > 0 ? n : 1;
+    std::vector<double> proj(n);
+    for (int it = 0; it < 30; ++it) {
+        std::fill(w.begin(), w.end(), 0.0);
+        for (int i = 0; i < n; ++i) {
+            const float *x = &s->sample[(size_t)i * d];
+            double p = 0.0;
+            for (int j = 0; j < d; ++j) p += (x[j] - mean[j]) * v[j];
+            for (int j = 0; j < d; ++j) w[j] += p * (x[j] - mean[j]);
+        }
+        double nrm = 0.0;
+        for (double x : w) nrm += x * x;
+        nrm = std::sqrt(nrm);
+        if (!(nrm > 0.0)) break;  // no spread: keep the current direction
+        for (int j = 0; j < d; ++j) v[j] = w[j] / nrm;
+    }
+    double lo = 0.0, hi = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double p = 0.0;
+        for (int j = 0; j < d; ++j) p += (s->sample[(size_t)i * d + j] - mean[j]) * v[j];
+        lo = i == 0 || p < lo ? p : lo;
+        hi = i == 0 || p > hi ? p : hi;
+    }
+    const double margin = 0.1 * (hi - lo);
+    s->order_lo = (float)(lo - margin);
+    s->order_scale = hi > lo ? (float)(kOrderBins / (hi - lo + 2 * margin)) : 0.0f;
+    std::vector<float> dm(2 * (size_t)d);
+    for (int j = 0; j < d; ++j) {
+        dm[j] = (float)v[j];
+        dm[d + j] = (float)mean[j];
+    }
+    int rc = upload(s->pdir, dm.data(), dm.size(), s->stream);
+    if (rc) return rc;
+    GSX_CUDA(cudaStreamSynchronize(s->stream));
+    return GSX_OK;
+}
+
 // Enqueues one batch on `st`; nothing is synchronised.
 int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int32_t *d_ef, const int32_t *d_k,
             int kmax, int efmax, int32_t *d_ids, float *d_dis, int32_t *d_cmps, bool single, cudaStream_t st,
@@ -241,6 +286,16 @@ int enqueue(gsx_searcher *s, const float *d_q, int nq, int k, int ef, const int3
     bv.status = s->status.as<int32_t>();
     bv.counter = s->counters.as<unsigned>();
     bv.overflow = s->counters.as<unsigned>() + 1;
+    // more queries than resident warps: run them sorted along the base data's principal direction,
+    // so that the queries in flight together touch nearby parts of the index
+    if (!single && s->pdir.p && !(s->tuning.prefetch & kNoBatchOrder) &&
+        nq > cfg.max_blocks * cfg.warps_per_block) {
+        if ((rc = s->qkeys.ensure((size_t)nq * 4))) return rc;
+        if ((rc = s->qorder.ensure((size_t)nq * 4))) return rc;
+        GSX_CUDA(launch_batch_order(d_q, nq, s->ix.d, s->pdir.as<float>(), s->order_lo, s->order_scale,
+                                    s->qkeys.as<uint32_t>(), s->qorder.as<int32_t>(), st));
+        bv.order = s->qorder.as<int32_t>();
+    }
     // one global visited table per resident warp of this launch shape
     const int sbits = spill_bits_for(s, cfg);
     const size_t slots = (size_t)cfg.max_blocks * cfg.warps_per_block;
@@ -565,7 +620,7 @@ void gsx_searcher_destroy(gsx_searcher *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->q, &s->ids,
                       &s->dis, &s->status, &s->cmps, &s->efp, &s->kp, &s->order, &s->counters, &s->gtab.buf,
-                      &s->spill.buf, &s->dist_out, &s->dist_ids})
+                      &s->spill.buf, &s->dist_out, &s->dist_ids, &s->pdir, &s->qkeys, &s->qorder})
         b->release();
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -612,6 +667,7 @@ int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t
         const int r = (int)(rng() % (uint32_t)n);
         std::memcpy(&s->sample[(size_t)i * dim], data + (size_t)r * dim, (size_t)dim * 4);
     }
+    if ((rc = batch_order_setup(s))) return rc;
     s->has_data = true;
     return GSX_OK;
 }
@@ -683,7 +739,7 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
     if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
         return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
                     kMinTableBits);
-    if (t->prefetch < 0 || t->prefetch > 15) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 15]");
+    if (t->prefetch < 0 || t->prefetch > 31) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 31]");
     if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
         return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
     s->tuning = *t;

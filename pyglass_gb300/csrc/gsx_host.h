@@ -88,6 +88,8 @@ struct gsx_searcher {
     // per-call scratch (device)
     gsx::DevBuf q, ids, dis, status, cmps, efp, kp, order, counters, dist_out, dist_ids;
     gsx::SpillTables spill, gtab;  // per-warp spill tables; whole-graph tables of the exact re-run
+    gsx::DevBuf pdir, qkeys, qorder;  // batch order: direction + mean (2d floats), per-batch keys/order
+    float order_lo = 0.0f, order_scale = 0.0f;
     // host copies for reporting
     std::vector<int32_t> h_cmps, h_status;
     double last_avg_cmps = 0.0;

@@ -21,6 +21,9 @@ constexpr int kPrefetchNeighbours = 4;  // tuning.prefetch bit: L1 prefetch of e
                                         // before its visited check
 constexpr int kNoStageCodes = 8;     // tuning.prefetch bit: do not stage neighbour code rows in shared
                                      // memory during the visited check (SQ kinds, rows <= 128 bytes)
+constexpr int kNoBatchOrder = 16;    // tuning.prefetch bit: run large batches in index order instead of
+                                     // sorted by their principal-direction projection
+constexpr int kOrderBins = 2048;     // bins of that sort
 
 // Device-resident index, as the kernels see it.
 struct IndexView {
@@ -104,6 +107,11 @@ int search_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg);
 cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, int d, int dalign, int csize, float p0,
                           float p1, uint8_t *out, cudaStream_t st);
 cudaError_t launch_pad_rows(const float *data, int64_t n, int d, int dalign, float *out, cudaStream_t st);
+
+// Work order of a batch (order_kernel.cu): order[0..nq) = the queries sorted by the bin of their
+// projection (q - mean) . dir; dirmean = dir[d] then mean[d]; keys = nq words of scratch.
+cudaError_t launch_batch_order(const float *q, int nq, int d, const float *dirmean, float lo, float scale,
+                               uint32_t *keys, int32_t *order, cudaStream_t st);
 cudaError_t launch_distances(const IndexView &ix, int refine, const float *queries, int nq, const int32_t *ids,
                              int m, double *out, cudaStream_t st);
 

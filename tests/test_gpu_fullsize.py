@@ -42,3 +42,24 @@ def test_clusters1m_sq4u_refine_matches_oracle(gpu, oracle, workload):
         assert np.all(np.diff(gd, axis=1) >= 0)
         assert np.all((gi >= 0) & (gi < base.shape[0]))
         assert all(len(set(r)) == r.size for r in gi)
+
+
+def test_batch_order_changes_no_result(gpu, workload):
+    """Batches larger than one wave of resident warps run sorted along the base data's principal
+    direction; in index order (tuning bit 16) every id, distance and distance count is the same."""
+    base, q = workload
+    s = gpu.Searcher(gpu.Graph(*FOUND), base, "L2", "SQ4U", "FP32")
+    s.set_ef(32)
+    qq = np.concatenate([q, q[::-1]])  # 20,000 queries: more than one wave on any GPU
+    try:
+        a_ids, a_dis = s.batch_search(qq, 10)
+        a_cmps = s.get_last_search_dist_cmps()
+        s.set_tuning(0, 0, 0, 16, 0)
+        b_ids, b_dis = s.batch_search(qq, 10)
+        b_cmps = s.get_last_search_dist_cmps()
+    finally:
+        s.set_tuning(0, 0, 0, 0, 0)
+    np.testing.assert_array_equal(a_ids, b_ids)
+    np.testing.assert_array_equal(a_dis, b_dis)
+    assert a_cmps == b_cmps
+    np.testing.assert_array_equal(a_ids[: q.shape[0]], a_ids[q.shape[0]:][::-1])
