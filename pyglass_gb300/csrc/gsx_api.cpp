@@ -95,43 +95,63 @@ int layout(int kind, int d, int *dalign, int *csize) {
     return GSX_OK;
 }
 
-// r-th smallest of v (0-based), on a private copy.
-float kth(std::vector<float> &v, int64_t r) {
-    std::nth_element(v.begin(), v.begin() + r, v.end());
-    return v[(size_t)r];
+// r-th smallest (0-based) of two ranks among x[0..n) on the device: radix select over the
+// order-preserving float keys, 8 bits a pass, both ranks in the same sweeps.
+int device_kth2(const float *x, int64_t n, int64_t r0, int64_t r1, unsigned *scratch, cudaStream_t st, float *v0,
+                float *v1) {
+    uint32_t prefix[2] = {0u, 0u}, mask = 0u;
+    int64_t rank[2] = {r0, r1};
+    std::vector<unsigned> h(512);
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        GSX_CUDA(launch_radix_hist2(x, n, prefix[0], prefix[1], mask, shift, scratch, st));
+        GSX_CUDA(cudaMemcpyAsync(h.data(), scratch, 512 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        GSX_CUDA(cudaStreamSynchronize(st));
+        for (int sel = 0; sel < 2; ++sel) {
+            int b = 0;
+            while (b < 255 && rank[sel] >= (int64_t)h[sel * 256 + b]) rank[sel] -= h[sel * 256 + b++];
+            prefix[sel] |= (uint32_t)b << shift;
+        }
+        mask |= 255u << shift;
+    }
+    *v0 = float_of_key(prefix[0]);
+    *v1 = float_of_key(prefix[1]);
+    return GSX_OK;
 }
 
 // Calibrator training (calibrator.hpp:481-514, quant/utils.hpp:584-603, sq8u_quant.hpp:240,
-// sq4u_quant.hpp:307-309).  find_minmax keeps the top = int64(nitems*ratio)+1 smallest / largest
-// values; the result is the top-th smallest and top-th largest.
-void calibrate(int kind, int metric, const float *data, int64_t n, int d, float *p) {
+// sq4u_quant.hpp:307-309) on the base data already on the device (`x`, n*d floats).  find_minmax
+// keeps the top = int64(nitems*ratio)+1 smallest / largest values; the result is the top-th
+// smallest and top-th largest.
+int calibrate(int kind, int metric, const float *x, int64_t n, int d, float *p, DevBuf &scratch, cudaStream_t st) {
     p[0] = p[1] = 0.0f;
+    if (kind != K_SQ8U && kind != K_SQ4U) return GSX_OK;
+    int rc = scratch.ensure(512 * sizeof(unsigned));
+    if (rc) return rc;
+    unsigned *w = scratch.as<unsigned>();
     if (kind == K_SQ8U) {
         const int64_t nitems = n * d;
+        unsigned mm[2];
+        GSX_CUDA(launch_minmax_keys(x, nitems, metric == M_L2 ? 0 : 1, w, st));
+        GSX_CUDA(cudaMemcpyAsync(mm, w, sizeof(mm), cudaMemcpyDeviceToHost, st));
+        GSX_CUDA(cudaStreamSynchronize(st));
         if (metric == M_L2) {
-            float mn = data[0], mx = data[0];
-            for (int64_t i = 1; i < nitems; ++i) {
-                mn = data[i] < mn ? data[i] : mn;
-                mx = data[i] > mx ? data[i] : mx;
-            }
-            p[0] = mn;
-            p[1] = mx - mn;
+            p[0] = float_of_key(mm[0]);
+            p[1] = float_of_key(mm[1]) - p[0];
         } else {
-            float mx = 0.0f;
-            for (int64_t i = 0; i < nitems; ++i) mx = std::fabs(data[i]) > mx ? std::fabs(data[i]) : mx;
-            p[0] = mx;
+            // the symmetric calibrator starts from 0: |x| >= 0, so the largest |x| (or 0 for all-zero data)
+            p[0] = float_of_key(mm[1]);
         }
-    } else if (kind == K_SQ4U) {
-        int64_t nitems = (int64_t)((float)(n * (int64_t)d) * 0.1f);
-        if (nitems < 1) nitems = 1;
-        int64_t top = (int64_t)((float)nitems * 0.01f) + 1;
-        if (top > nitems) top = nitems;
-        std::vector<float> v(data, data + nitems);
-        const float mn = kth(v, top - 1);
-        const float mx = kth(v, nitems - top);
-        p[0] = mn;
-        p[1] = mx - mn;
+        return GSX_OK;
     }
+    int64_t nitems = (int64_t)((float)(n * (int64_t)d) * 0.1f);
+    if (nitems < 1) nitems = 1;
+    int64_t top = (int64_t)((float)nitems * 0.01f) + 1;
+    if (top > nitems) top = nitems;
+    float mn = 0.0f, mx = 0.0f;
+    if ((rc = device_kth2(x, nitems, top - 1, nitems - top, w, st, &mn, &mx))) return rc;
+    p[0] = mn;
+    p[1] = mx - mn;
+    return GSX_OK;
 }
 
 int set_device(const gsx_searcher *s) {
@@ -637,13 +657,13 @@ int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t
     IndexView &ix = s->ix;
     ix.d = dim;
     layout(s->kind, dim, &ix.dalign, &ix.csize);
+    cudaStream_t st = s->stream;
+    DevBuf raw, scratch;
+    if ((rc = upload(raw, data, (size_t)n * dim, st))) return rc;
     float p[2];
-    calibrate(s->kind, s->metric, data, n, dim, p);
+    if ((rc = calibrate(s->kind, s->metric, raw.as<float>(), n, dim, p, scratch, st))) return rc;
     ix.p0 = p[0];
     ix.p1 = p[1];
-    cudaStream_t st = s->stream;
-    DevBuf raw;
-    if ((rc = upload(raw, data, (size_t)n * dim, st))) return rc;
     if ((rc = s->codes.ensure((size_t)n * ix.csize))) return rc;
     if (s->kind == K_FP32) {
         GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.dalign, s->codes.as<float>(), st));

@@ -108,6 +108,15 @@ cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, in
                           float p1, uint8_t *out, cudaStream_t st);
 cudaError_t launch_pad_rows(const float *data, int64_t n, int d, int dalign, float *out, cudaStream_t st);
 
+// Calibration on the device (calib_kernel.cu).  Keys are order-preserving images of floats.
+// launch_minmax_keys: out[0..1] = min and max key of x[0..n) (of |x| when absval); launch_radix_hist2:
+// hist[0..511] = for s = 0, 1 the counts by 8-bit digit at `shift` of the keys matching prefix_s on
+// mask (out and hist are device words).  float_of_key inverts a key.
+cudaError_t launch_minmax_keys(const float *x, int64_t n, int absval, unsigned *out, cudaStream_t st);
+cudaError_t launch_radix_hist2(const float *x, int64_t n, uint32_t prefix0, uint32_t prefix1, uint32_t mask, int shift,
+                               unsigned *hist, cudaStream_t st);
+float float_of_key(uint32_t k);
+
 // Work order of a batch (order_kernel.cu): order[0..nq) = the queries sorted by the bin of their
 // projection (q - mean) . dir; dirmean = dir[d] then mean[d]; keys = nq words of scratch.
 cudaError_t launch_batch_order(const float *q, int nq, int d, const float *dirmean, float lo, float scale,
