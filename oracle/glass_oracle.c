@@ -24,6 +24,8 @@ int go_layout(int kind, int d, int *dalign, int *csize) {
         case GO_SQ8U: align = 64; nbits = 8; break;   /* sq8u_quant.hpp:14  Quantizer<metric,64,8> */
         case GO_SQ4U: align = 128; nbits = 4; break;  /* sq4u_quant.hpp:13  Quantizer<metric,128,4> */
         case GO_E5M2: align = 16; nbits = 8; break;   /* e5m2_quant.hpp:11  Quantizer<metric,16,8> */
+        case GO_FP16: align = 16; nbits = 16; break;  /* fp16_quant.hpp:10-16 (no AVX512-FP16 build macro) */
+        case GO_BF16: align = 16; nbits = 16; break;  /* bf16_quant.hpp:9-15 (no AVX512-BF16 build macro) */
         case GO_FP32: align = 16; nbits = 32; break;  /* fp32_quant.hpp:8   Quantizer<metric,16,32> */
         default: return -1;
     }
@@ -182,11 +184,27 @@ static float f16_to_f32(uint16_t h) {
     return f;
 }
 
+/* bf16 on x86: round to nearest with ties away from zero on the bit pattern, (bits + 0x8000) >> 16
+ * (helpa/types.hpp:20,34-35,72-75); decode = bits << 16 (types.hpp:50-58). */
+static inline uint16_t bf16_encode(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return (uint16_t)((u + 0x8000u) >> 16);
+}
+static inline float bf16_decode(uint16_t h) {
+    uint32_t u = (uint32_t)h << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
 /* e5m2 code = high byte of the fp16 value (glass/types.hpp:19-32); decode = byte<<8 as fp16. */
 static inline uint8_t e5m2_encode(float x) { return (uint8_t)(f32_to_f16_rne(x) >> 8); }
 static inline float e5m2_decode(uint8_t b) { return f16_to_f32((uint16_t)((uint16_t)b << 8)); }
 
-static void encode_row(int kind, int metric, const float *p, const float *x, int d, int csize, uint8_t *out) {
+/* `avail` = floats readable from x (the rest of the data array): FP16 rows read past their end, below. */
+static void encode_row(int kind, int metric, const float *p, const float *x, int d, int csize, int64_t avail,
+                       uint8_t *out) {
     memset(out, 0, (size_t)csize);
     if (kind == GO_SQ8U) {
         if (metric == GO_L2) {
@@ -201,6 +219,19 @@ static void encode_row(int kind, int metric, const float *p, const float *x, int
         }
     } else if (kind == GO_E5M2) {
         for (int j = 0; j < d; ++j) out[j] = e5m2_encode(x[j]);
+    } else if (kind == GO_FP16) {
+        /* helpa::fp32_to_fp16 (x86/data_convert.hpp:17-38): vcvtps2ph (nearest-even) over 16-wide blocks
+         * while i < d, so the block that holds the row's tail also converts the floats that follow it
+         * in the data array into the padding (the next row's first dalign-d values); the last row's
+         * padding would read past the array and is left zero here */
+        const int dalign = csize / 2;
+        for (int j = 0; j < dalign; ++j) {
+            const float v = j < d ? x[j] : ((int64_t)j < avail ? x[j] : 0.0f);
+            uint16_t h = (j < d || (int64_t)j < avail) ? f32_to_f16_rne(v) : 0;
+            memcpy(out + 2 * j, &h, 2);
+        }
+    } else if (kind == GO_BF16) {                    /* BF16Quantizer::encode: bf16(float) per element */
+        for (int j = 0; j < d; ++j) { uint16_t h = bf16_encode(x[j]); memcpy(out + 2 * j, &h, 2); }
     } else {
         memcpy(out, x, sizeof(float) * (size_t)d);
     }
@@ -210,14 +241,15 @@ void go_encode(int kind, int metric, const float *p, const float *data, int64_t 
     int dalign, csize;
     go_layout(kind, d, &dalign, &csize);
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < n; ++i) encode_row(kind, metric, p, data + i * d, d, csize, codes + i * csize);
+    for (int64_t i = 0; i < n; ++i)
+        encode_row(kind, metric, p, data + i * d, d, csize, (n - i) * (int64_t)d, codes + i * csize);
 }
 
 int go_encode_query(int kind, int metric, const float *p, const float *q, int d, void *out) {
     int dalign, csize;
     go_layout(kind, d, &dalign, &csize);
     if (kind == GO_SQ8U || kind == GO_SQ4U) {
-        encode_row(kind, metric, p, q, d, csize, (uint8_t *)out);
+        encode_row(kind, metric, p, q, d, csize, d, (uint8_t *)out);
         return csize;
     }
     memset(out, 0, sizeof(float) * (size_t)dalign);  /* computer.hpp:56-59 (zero-filled align_alloc) */
@@ -277,6 +309,17 @@ double go_distance(int kind, int metric, const void *qenc, const uint8_t *code, 
         }
         float r = reduce16_glass(acc);
         return metric == GO_L2 ? (double)r : (double)(-r);
+    } else if (kind == GO_FP16 || kind == GO_BF16) {
+        /* l2a_fp32_fp16 / dota_fp32_fp16 and the bf16 twins (helpa x86/l2_impl.hpp:74-107, 145-181,
+         * dot_impl.hpp:74-83, 139-150): the fp32 query against the exactly widened code, 16 fused
+         * accumulators, helpa's reduction */
+        for (int i = 0; i < dalign; ++i) {
+            uint16_t h;
+            memcpy(&h, code + 2 * i, 2);
+            float y = kind == GO_FP16 ? f16_to_f32(h) : bf16_decode(h);
+            if (metric == GO_L2) { float t = q[i] - y; acc[i & 15] = fmaf(t, t, acc[i & 15]); }
+            else acc[i & 15] = fmaf(q[i], y, acc[i & 15]);
+        }
     } else {
         const float *y = (const float *)code;
         for (int i = 0; i < dalign; ++i) {

@@ -22,10 +22,10 @@ ORACLE_SO = os.path.join(HERE, "_build", "libglass_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libglass_ref.so")
 REFERENCE_DIR = os.environ.get("GLASS_REFERENCE_DIR", "/root/reference")
 
-KIND = {"FP32": 0, "E5M2": 3, "SQ8U": 4, "SQ4U": 7}
+KIND = {"FP32": 0, "FP16": 1, "BF16": 2, "E5M2": 3, "SQ8U": 4, "SQ4U": 7}
 METRIC = {"L2": 0, "IP": 1}
 # get_refine_factor (glass/searcher/graph_searcher.hpp:227-238) for the quantizers in scope
-REFINE_FACTOR = {"SQ8U": 1.5, "SQ4U": 1.5, "E5M2": 1.0, "FP32": 1.0}
+REFINE_FACTOR = {"SQ8U": 1.5, "SQ4U": 1.5, "E5M2": 1.0, "FP32": 1.0, "FP16": 1.0, "BF16": 1.0}
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")

@@ -50,6 +50,14 @@ int with_quant(const std::string &quant, const std::string &metric, int d, Fn &&
         if (l2) { glass::FP32Quantizer<Metric::L2> q(d); return fn(q); }
         glass::FP32Quantizer<Metric::IP> q(d); return fn(q);
     }
+    if (quant == "FP16") {
+        if (l2) { glass::FP16Quantizer<Metric::L2> q(d); return fn(q); }
+        glass::FP16Quantizer<Metric::IP> q(d); return fn(q);
+    }
+    if (quant == "BF16") {
+        if (l2) { glass::BF16Quantizer<Metric::L2> q(d); return fn(q); }
+        glass::BF16Quantizer<Metric::IP> q(d); return fn(q);
+    }
     return -1;
 }
 

@@ -7,7 +7,7 @@ Needs the reference checkout (oracle/_ref is compiled from it by oracle/Makefile
 The inputs are regenerated from seeds (pyglass_gb300.datasets, identical bytes on x86 and
 aarch64), so only graphs and outputs are stored.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--rebuild-graphs]
 """
 
 import hashlib
@@ -30,7 +30,10 @@ def main():
     base, queries = spec.base(), spec.queries()
     for name, (itype, Rdeg, L) in spec.GRAPHS.items():
         path = os.path.join(HERE, f"{name}.glass")
-        R.build_graph(itype, base, "L2", "FP32", Rdeg, L, path)
+        # the builders are multi-threaded and not deterministic: keep the committed graphs, so that
+        # adding cases does not change the existing ones
+        if not os.path.exists(path) or "--rebuild-graphs" in sys.argv:
+            R.build_graph(itype, base, "L2", "FP32", Rdeg, L, path)
     out = {}
     rng = np.random.default_rng(5)
     ids = rng.integers(0, base.shape[0], size=(spec.NQ_DIST, 40)).astype(np.int32)
