@@ -73,10 +73,12 @@ namespace {
 
 // quantizer_map (glass/quant/quant.hpp:25-43); operator[] on an unknown key yields FP32.
 int parse_quant(const std::string &q, int *kind) {
-    static const char *unsupported[] = {"FP16", "BF16", "SQ8", "SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "SQ2U", "PQ8"};
+    static const char *unsupported[] = {"SQ8", "SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "SQ2U", "PQ8"};
     if (q == "SQ8U") *kind = K_SQ8U;
     else if (q == "SQ4U") *kind = K_SQ4U;
     else if (q == "E5M2") *kind = K_E5M2;
+    else if (q == "FP16") *kind = K_FP16;
+    else if (q == "BF16") *kind = K_BF16;
     else {
         for (const char *u : unsupported)
             if (q == u) return fail(GSX_ERR_UNSUPPORTED, "quantizer %s is outside the GPU search path", u);
@@ -90,6 +92,9 @@ int layout(int kind, int d, int *dalign, int *csize) {
     if (kind == K_SQ8U) { align = 64; nbits = 8; }
     else if (kind == K_SQ4U) { align = 128; nbits = 4; }
     else if (kind == K_E5M2) { align = 16; nbits = 8; }
+    // fp16_quant.hpp:10-16, bf16_quant.hpp:9-15: align 16 unless built with AVX512-FP16/BF16 macros that
+    // the reference's build never defines
+    else if (kind == K_FP16 || kind == K_BF16) { align = 16; nbits = 16; }
     *dalign = (d + align - 1) / align * align;  // tensor.hpp:122-123
     *csize = *dalign * nbits / 8;
     return GSX_OK;
@@ -192,7 +197,7 @@ int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int tabl
     int bits = table_bits_override > 0 ? table_bits_override : (s->tuning.table_bits > 0 ? s->tuning.table_bits : kGlobalOnly);
     int wpb = single ? 1 : (s->tuning.warps_per_block > 0 ? s->tuning.warps_per_block : 4);
     int lpr = s->tuning.lanes_per_row > 0 ? s->tuning.lanes_per_row
-              : ((s->kind == K_E5M2 || s->kind == K_FP32) ? 4 : (s->ix.csize > 256 ? 4 : 1));
+              : (is_float_kind(s->kind) ? 4 : (s->ix.csize > 256 ? 4 : 1));
     WarpLayout L;
     if (bits == kGlobalOnly) {
         // no shared-memory table: every query keeps its visited set in its warp's global table
@@ -763,7 +768,7 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
     if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
         return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
     s->tuning = *t;
-    if ((s->kind == K_E5M2 || s->kind == K_FP32) && s->tuning.lanes_per_row == 2) s->tuning.lanes_per_row = 4;
+    if (is_float_kind(s->kind) && s->tuning.lanes_per_row == 2) s->tuning.lanes_per_row = 4;
     return GSX_OK;
 }
 
@@ -786,7 +791,7 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
     if ((rc = s->dis.ensure((size_t)nq * k * 4))) return rc;
     const gsx_tuning saved = s->tuning;
     const int base_bits = default_table_bits(s, std::max(s->ef, kin_of(s, k)));
-    std::vector<int> lprs = (s->kind == K_E5M2 || s->kind == K_FP32) ? std::vector<int>{1, 4} : std::vector<int>{1, 2, 4};
+    std::vector<int> lprs = is_float_kind(s->kind) ? std::vector<int>{1, 4} : std::vector<int>{1, 2, 4};
     gsx_tuning best = saved;
     float best_ms = 1e30f;
     // visited sets in global tables only, or a small shared table in front; sparse global tables

@@ -210,10 +210,13 @@ __device__ __forceinline__ int32_t sq_finish(int32_t partial, int32_t qsq) {
 //   (a0+a1)+(a2+a3).
 // Reproducing that order gives the same bits as the x86 reference.  With LPR lanes per row each
 // lane owns NA = 16/LPR consecutive accumulators; the first tree levels cross lanes by shuffles.
-template <bool E5M2, int METRIC, int LPR>
+// FP16 and BF16 codes (helpa x86 l2a/dota_fp32_fp16, _fp32_bf16: the same 16 fused accumulators and
+// helpa reduction as FP32) widen exactly to fp32 before the arithmetic.
+template <int KIND, int METRIC, int LPR>
 __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_bytes, int nsteps, int sub,
                                             const float *fq, bool active) {
     constexpr int NA = 16 / LPR;
+    constexpr bool E5M2 = KIND == K_E5M2;
     float a[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) a[i] = 0.0f;
@@ -221,7 +224,25 @@ __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_byte
         for (int m = 0; m < nsteps; ++m) {
             const int base = 16 * m + NA * sub;
             float y[NA];
-            if constexpr (E5M2) {
+            if constexpr (KIND == K_FP16 || KIND == K_BF16) {
+                static_assert(NA == 4 || NA == 16, "16-bit engines support 1 or 4 lanes per row");
+                uint32_t ws[NA / 2];
+                if constexpr (NA == 16) {
+                    const uint4 *r = reinterpret_cast<const uint4 *>(row_bytes + 2 * base);
+                    const uint4 w0 = __ldg(r), w1 = __ldg(r + 1);
+                    ws[0] = w0.x; ws[1] = w0.y; ws[2] = w0.z; ws[3] = w0.w;
+                    ws[4] = w1.x; ws[5] = w1.y; ws[6] = w1.z; ws[7] = w1.w;
+                } else {
+                    const uint2 w = __ldg(reinterpret_cast<const uint2 *>(row_bytes + 2 * base));
+                    ws[0] = w.x; ws[1] = w.y;
+                }
+#pragma unroll
+                for (int i = 0; i < NA; ++i) {
+                    const uint32_t h = (ws[i >> 1] >> (16 * (i & 1))) & 0xffffu;
+                    if constexpr (KIND == K_FP16) y[i] = __half2float(__ushort_as_half((unsigned short)h));
+                    else y[i] = __uint_as_float(h << 16);
+                }
+            } else if constexpr (E5M2) {
                 if constexpr (NA == 16) {
                     uint4 w = __ldg(reinterpret_cast<const uint4 *>(row_bytes + base));
                     uint32_t ws[4] = {w.x, w.y, w.z, w.w};

@@ -415,7 +415,7 @@ __device__ __forceinline__ void compute_dists(const IndexView &ix, WarpState &w,
             key = key_of(sq_finish<KIND, METRIC, LPR>(part, qsq));
         } else {
             const uint8_t *row = ix.codes + (size_t)id * (size_t)ix.csize;
-            float dv = float_dist<KIND == K_E5M2, METRIC, LPR>(row, ix.dalign >> 4, sub, w.fq, act);
+            float dv = float_dist<KIND, METRIC, LPR>(row, ix.dalign >> 4, sub, w.fq, act);
             key = key_of(dv);
         }
         if (act && sub == 0) w.cand_key[j] = key;
@@ -433,7 +433,7 @@ __device__ __forceinline__ void refine_dists(const IndexView &ix, const int32_t 
         const bool act = j < m;
         const int id = act ? ids[j] : 0;
         const uint8_t *row = reinterpret_cast<const uint8_t *>(ix.r_codes + (size_t)id * (size_t)ix.r_dalign);
-        float dv = float_dist<false, METRIC, 4>(row, ix.r_dalign >> 4, sub, fq, act);
+        float dv = float_dist<K_FP32, METRIC, 4>(row, ix.r_dalign >> 4, sub, fq, act);
         if (act && sub == 0) out[j] = dv;
     }
     __syncwarp();
@@ -927,6 +927,12 @@ auto dispatch(int kind, int metric, int lpr, A &&...a) {
         case K_E5M2:
             if (ip) return lpr == 1 ? F<K_E5M2, M_IP, 1>::run(a...) : F<K_E5M2, M_IP, 4>::run(a...);
             return lpr == 1 ? F<K_E5M2, M_L2, 1>::run(a...) : F<K_E5M2, M_L2, 4>::run(a...);
+        case K_FP16:
+            if (ip) return lpr == 1 ? F<K_FP16, M_IP, 1>::run(a...) : F<K_FP16, M_IP, 4>::run(a...);
+            return lpr == 1 ? F<K_FP16, M_L2, 1>::run(a...) : F<K_FP16, M_L2, 4>::run(a...);
+        case K_BF16:
+            if (ip) return lpr == 1 ? F<K_BF16, M_IP, 1>::run(a...) : F<K_BF16, M_IP, 4>::run(a...);
+            return lpr == 1 ? F<K_BF16, M_L2, 1>::run(a...) : F<K_BF16, M_L2, 4>::run(a...);
         default:
             if (ip) return lpr == 1 ? F<K_FP32, M_IP, 1>::run(a...) : F<K_FP32, M_IP, 4>::run(a...);
             return lpr == 1 ? F<K_FP32, M_L2, 1>::run(a...) : F<K_FP32, M_L2, 4>::run(a...);
@@ -972,7 +978,7 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     L->acc_key = off; off += kMaxDegree * 4;
     L->acc_id = off; off += kMaxDegree * 4;
     int fq = ix.d;
-    if (ix.kind == K_E5M2 || ix.kind == K_FP32) fq = fq > ix.dalign ? fq : ix.dalign;
+    if (is_float_kind(ix.kind)) fq = fq > ix.dalign ? fq : ix.dalign;
     if (ix.has_refine) fq = fq > ix.r_dalign ? fq : ix.r_dalign;
     fq = up(fq, 16);
     L->fq = off; off += fq * 4;
