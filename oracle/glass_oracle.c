@@ -498,8 +498,9 @@ typedef struct { int32_t id; float d; } nb_t;
 static int nb_less(nb_t a, nb_t b) { return a.d < b.d || (a.d == b.d && a.id < b.id); }  /* neighbor.hpp:205-207 */
 
 static float refine_dist(const go_index *ix, const float *qpad, int32_t id) {
-    return (float)go_distance(GO_FP32, ix->metric, qpad, (const uint8_t *)(ix->r_codes + (int64_t)id * ix->r_dalign),
-                              ix->r_dalign);
+    const int esize = ix->r_kind == GO_FP16 ? 2 : 4;
+    const uint8_t *row = (const uint8_t *)ix->r_codes + (int64_t)id * ix->r_dalign * esize;
+    return (float)go_distance(ix->r_kind == GO_FP16 ? GO_FP16 : GO_FP32, ix->metric, qpad, row, ix->r_dalign);
 }
 
 void go_search(const go_index *ix, const float *queries, int64_t nq, int k, int ef, const int32_t *ef_per_query,

@@ -73,10 +73,11 @@ typedef struct {
     int kind, metric, d, dalign, csize;
     float p[2];
     const uint8_t *codes;
-    int has_refine;         /* FP32 refiner present (refiner.hpp:15-111) */
+    int has_refine;         /* refiner present (refiner.hpp:15-111) */
     float refine_factor;    /* get_refine_factor (graph_searcher.hpp:227-238) */
     int r_dalign;
-    const float *r_codes;   /* N*r_dalign fp32 rows */
+    const void *r_codes;    /* N*r_dalign rows of the refine quantizer: fp32, or fp16 when r_kind = GO_FP16 */
+    int r_kind;             /* GO_FP32 or GO_FP16 (make_refiner, graph_searcher.hpp:240-254) */
 } go_index;
 
 /*

@@ -61,6 +61,7 @@ class _GoIndex(C.Structure):
         ("g", C.POINTER(_GoGraph)), ("kind", C.c_int), ("metric", C.c_int), ("d", C.c_int),
         ("dalign", C.c_int), ("csize", C.c_int), ("p", C.c_float * 2), ("codes", C.c_void_p),
         ("has_refine", C.c_int), ("refine_factor", C.c_float), ("r_dalign", C.c_int), ("r_codes", C.c_void_p),
+        ("r_kind", C.c_int),
     ]
 
 
@@ -157,12 +158,18 @@ class Searcher:
         self._ix.p[0], self._ix.p[1] = float(self.q.params[0]), float(self.q.params[1])
         self._ix.codes = self.q.codes.ctypes.data
         self.refine = None
-        if refine_quant:
-            self.refine = Quant("FP32", metric, data)
+        # make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer
+        # map does not know -> FP32 store; any other known quantizer name -> no refiner
+        known = {"FP32", "FP16", "BF16", "E5M2", "SQ8U", "SQ8", "SQ6", "SQ4U", "SQ4UA", "SQ4", "SQ8P", "SQ1",
+                 "SQ2U", "PQ8"}
+        if refine_quant and (refine_quant in ("FP16", "FP32") or refine_quant not in known):
+            rq = "FP16" if refine_quant == "FP16" else "FP32"
+            self.refine = Quant(rq, metric, data)
             self._ix.has_refine = 1
             self._ix.refine_factor = REFINE_FACTOR[quantizer]
             self._ix.r_dalign = self.refine.dalign
             self._ix.r_codes = self.refine.codes.ctypes.data
+            self._ix.r_kind = KIND[rq]
         self.last_cmps = None
 
     def set_ef(self, ef: int) -> None:

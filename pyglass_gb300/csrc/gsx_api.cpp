@@ -583,18 +583,29 @@ int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quanti
     int rc = parse_quant(quantizer ? quantizer : "", &kind);
     if (rc) return rc;
     const std::string rq = refine_quant ? refine_quant : "";
+    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ4U, 1.0 otherwise (in which
+    // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
+    const float factor = (kind == K_SQ8U || kind == K_SQ4U) ? 1.5f : 1.0f;
+    // make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer map
+    // does not know -> FP32 store; SQ8U / SQ8 -> their own refiners; any other known name -> none
     int rkind = K_FP32;
-    if (!rq.empty() && (rc = parse_quant(rq, &rkind))) return rc;
-    if (!rq.empty() && rkind != K_FP32)
-        return fail(GSX_ERR_UNSUPPORTED, "refine quantizer %s is outside the GPU search path", rq.c_str());
+    bool refiner = false;
+    if (!rq.empty()) {
+        static const char *no_refiner[] = {"BF16", "E5M2", "SQ6", "SQ4U", "SQ4UA", "SQ4", "SQ8P", "SQ1", "SQ2U", "PQ8"};
+        refiner = true;
+        if (rq == "FP16") rkind = K_FP16;
+        for (const char *u : no_refiner)
+            if (rq == u) refiner = false;
+        if ((rq == "SQ8U" || rq == "SQ8") && factor != 1.0f)
+            return fail(GSX_ERR_UNSUPPORTED, "refine quantizer %s is outside the GPU search path", rq.c_str());
+        if (rq == "SQ8U" || rq == "SQ8") refiner = false;  // factor 1: the refiner only forwards
+    }
     auto *s = new gsx_searcher;
     s->kind = kind;
     // metric_map (common.hpp:13-19): unknown names fall on the default-constructed L2
     s->metric = (metric && std::string(metric) == "IP") ? M_IP : M_L2;
-    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ4U, 1.0 otherwise (in which
-    // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
-    const float factor = (kind == K_SQ8U || kind == K_SQ4U) ? 1.5f : 1.0f;
-    s->has_refine = (!rq.empty() && factor != 1.0f) ? 1 : 0;
+    s->has_refine = (refiner && factor != 1.0f) ? 1 : 0;
+    s->r_kind = rkind;
     s->refine_factor = factor;
     s->device = device;
     s->graph = std::move(graph->g);  // the Python Graph is moved from (python/bindings.cc:98)
@@ -678,12 +689,19 @@ int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t
     }
     if (s->has_refine) {
         ix.r_dalign = (dim + 15) / 16 * 16;
-        if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 4))) return rc;
-        GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.r_dalign, s->r_codes.as<float>(), st));
+        if (s->r_kind == K_FP16) {
+            if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 2))) return rc;
+            GSX_CUDA(launch_encode(K_FP16, s->metric, raw.as<float>(), n, dim, ix.r_dalign, ix.r_dalign * 2, 0.0f, 0.0f,
+                                   s->r_codes.as<uint8_t>(), st));
+        } else {
+            if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 4))) return rc;
+            GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.r_dalign, s->r_codes.as<float>(), st));
+        }
     }
     GSX_CUDA(cudaStreamSynchronize(st));
     ix.codes = s->codes.as<uint8_t>();
-    ix.r_codes = s->r_codes.as<float>();
+    ix.r_codes = s->r_codes.as<uint8_t>();
+    ix.r_kind = s->r_kind;
     // keep 1,000 sampled rows for optimize (graph_searcher.hpp:62-69)
     s->sample_n = std::min(1000, n);
     std::mt19937 rng(12345);

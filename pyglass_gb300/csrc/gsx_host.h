@@ -73,6 +73,7 @@ struct gsx_searcher {
     // create_searcher arguments
     int kind = gsx::K_FP32, metric = gsx::M_L2;
     int has_refine = 0;
+    int r_kind = gsx::K_FP32;  // refine store: FP32 or FP16 rows
     float refine_factor = 1.0f;
     int device = 0;
     int ef = 32;

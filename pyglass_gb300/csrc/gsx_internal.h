@@ -44,7 +44,8 @@ struct IndexView {
     int32_t has_refine;
     float refine_factor;
     int32_t r_dalign;
-    const float *r_codes;     // N*r_dalign fp32 rows
+    const uint8_t *r_codes;   // N*r_dalign rows of the refine quantizer (fp32, or fp16 when r_kind = K_FP16)
+    int32_t r_kind;           // K_FP32 or K_FP16
 };
 
 // One batched launch.

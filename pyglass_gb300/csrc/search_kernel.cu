@@ -423,7 +423,7 @@ __device__ __forceinline__ void compute_dists(const IndexView &ix, WarpState &w,
     __syncwarp();
 }
 
-// FP32 refine distance of cand_id[0..m) into cand_key (as float bits), 4 lanes per row.
+// Refine distance (FP32 or FP16 store) of ids[0..m) into out, 4 lanes per row.
 template <int METRIC>
 __device__ __forceinline__ void refine_dists(const IndexView &ix, const int32_t *ids, float *out, int m,
                                              const float *fq, int lane) {
@@ -432,8 +432,10 @@ __device__ __forceinline__ void refine_dists(const IndexView &ix, const int32_t 
         const int j = b + team;
         const bool act = j < m;
         const int id = act ? ids[j] : 0;
-        const uint8_t *row = reinterpret_cast<const uint8_t *>(ix.r_codes + (size_t)id * (size_t)ix.r_dalign);
-        float dv = float_dist<K_FP32, METRIC, 4>(row, ix.r_dalign >> 4, sub, fq, act);
+        const size_t esize = ix.r_kind == K_FP16 ? 2 : 4;
+        const uint8_t *row = ix.r_codes + (size_t)id * (size_t)ix.r_dalign * esize;
+        float dv = ix.r_kind == K_FP16 ? float_dist<K_FP16, METRIC, 4>(row, ix.r_dalign >> 4, sub, fq, act)
+                                       : float_dist<K_FP32, METRIC, 4>(row, ix.r_dalign >> 4, sub, fq, act);
         if (act && sub == 0) out[j] = dv;
     }
     __syncwarp();
@@ -829,7 +831,7 @@ __global__ void __launch_bounds__(256, IsIntKind<KIND>::value ? 4 : 2) search_ke
 }
 
 // ComputerImpl::operator() for a list of ids (computer.hpp:67-72): one warp per query, the same
-// query encoding and distance engines as the search.  refine=1 uses the FP32 refine store.
+// query encoding and distance engines as the search.  refine=1 uses the refine store.
 template <int KIND, int METRIC, int LPR>
 __global__ void __launch_bounds__(128) distance_kernel(IndexView ix, int refine, const float *queries, int nq,
                                                        const int32_t *ids, int m, double *out, WarpLayout L) {

@@ -12,7 +12,9 @@ QUANTS = [("SQ8U", "L2"), ("SQ8U", "IP"), ("SQ4U", "L2"), ("SQ4U", "IP"), ("E5M2
 # (quant, metric, refine)
 SEARCHERS = [("SQ8U", "L2", ""), ("SQ8U", "IP", ""), ("SQ4U", "L2", "FP32"), ("SQ4U", "IP", "FP32"),
              ("E5M2", "L2", ""), ("E5M2", "IP", ""), ("FP32", "L2", ""), ("FP32", "IP", ""), ("SQ8U", "L2", "FP32"),
-             ("FP16", "L2", ""), ("FP16", "IP", ""), ("BF16", "L2", ""), ("BF16", "IP", "")]
+             ("FP16", "L2", ""), ("FP16", "IP", ""), ("BF16", "L2", ""), ("BF16", "IP", ""),
+             # make_refiner: an FP16 store; a known quantizer without a refiner; a name the map lacks (FP32)
+             ("SQ4U", "L2", "FP16"), ("SQ8U", "IP", "FP16"), ("SQ4U", "L2", "BF16"), ("SQ4U", "IP", "FP64")]
 # (ef, k): includes k > ef, the case where search and batch_search differ (graph_searcher.hpp:134,152)
 EFK = [(16, 10), (40, 10), (8, 20)]
 
