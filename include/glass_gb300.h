@@ -66,11 +66,13 @@ void gsx_graph_destroy(gsx_graph *g);
 /* ---- searchers: GraphSearcherBase (glass/searcher/searcher_base.hpp:7-19) ---------------- */
 
 /* create_searcher(graph, metric, quantizer, refine_quant) (graph_searcher.hpp:256-391).
- * metric "L2" | "IP"; quantizer "SQ8U" | "SQ4U" | "E5M2" | "FP32" (an unknown name selects
- * FP32, as the reference's quantizer_map does); refine_quant "" or "FP32" (Refiner with
- * get_refine_factor, graph_searcher.hpp:227-254).  The graph's contents move into the searcher
- * (python/bindings.cc:98); *graph is left empty but must still be destroyed.  device = CUDA
- * ordinal. */
+ * metric "L2" | "IP"; quantizer "SQ8U" | "SQ4U" | "E5M2" | "FP32" | "FP16" | "BF16" (an unknown
+ * name selects FP32, as the reference's quantizer_map does; SQ8, SQ6, SQ4, SQ4UA, SQ8P, SQ2U, SQ1
+ * and PQ8 return GSX_ERR_UNSUPPORTED); refine_quant as make_refiner reads it
+ * (graph_searcher.hpp:227-254): "" none, "FP16" an FP16 store, "FP32" or a name the quantizer map
+ * lacks an FP32 store, any other known name no refiner; "SQ8U" / "SQ8" with an SQ quantizer return
+ * GSX_ERR_UNSUPPORTED.  The graph's contents move into the searcher (python/bindings.cc:98); *graph
+ * is left empty but must still be destroyed.  device = CUDA ordinal. */
 int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quantizer, const char *refine_quant,
                         int device, gsx_searcher **out);
 void gsx_searcher_destroy(gsx_searcher *s);
