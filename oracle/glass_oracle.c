@@ -23,6 +23,7 @@ int go_layout(int kind, int d, int *dalign, int *csize) {
     switch (kind) {
         case GO_SQ8U: align = 64; nbits = 8; break;   /* sq8u_quant.hpp:14  Quantizer<metric,64,8> */
         case GO_SQ4U: align = 128; nbits = 4; break;  /* sq4u_quant.hpp:13  Quantizer<metric,128,4> */
+        case GO_SQ2U: align = 256; nbits = 2; break;  /* sq2u_quant.hpp:11  Quantizer<metric,256,2> */
         case GO_E5M2: align = 16; nbits = 8; break;   /* e5m2_quant.hpp:11  Quantizer<metric,16,8> */
         case GO_FP16: align = 16; nbits = 16; break;  /* fp16_quant.hpp:10-16 (no AVX512-FP16 build macro) */
         case GO_BF16: align = 16; nbits = 16; break;  /* bf16_quant.hpp:9-15 (no AVX512-BF16 build macro) */
@@ -104,12 +105,13 @@ void go_train(int kind, int metric, const float *data, int64_t n, int d, float *
         } else {
             p[0] = find_absmax(data, nitems);     /* calibrator.hpp:511-514 */
         }
-    } else if (kind == GO_SQ4U) {
-        /* sq4u_quant.hpp:307-309: nitems = (int64)(n*d*0.1f) - an int64*float product - drop 1% */
+    } else if (kind == GO_SQ4U || kind == GO_SQ2U) {
+        /* sq4u_quant.hpp:307-309, sq2u_quant.hpp:27-29: nitems = (int64)(n*d*0.1f) - an int64*float
+         * product - then drop 1% (SQ4U) or 5% (SQ2U) at each end */
         int64_t nitems = (int64_t)((float)(n * (int64_t)d) * 0.1f);
         if (nitems < 1) nitems = 1;
         float mn, mx;
-        find_minmax(data, nitems, 0.01f, &mn, &mx);
+        find_minmax(data, nitems, kind == GO_SQ4U ? 0.01f : 0.05f, &mn, &mx);
         p[0] = mn;
         p[1] = mx - mn;
     }
@@ -217,6 +219,8 @@ static void encode_row(int kind, int metric, const float *p, const float *x, int
             uint8_t y = (uint8_t)affine_code(x[j], p[0], p[1], 15);
             out[j / 2] |= (j & 1) ? (uint8_t)(y << 4) : y;
         }
+    } else if (kind == GO_SQ2U) {                    /* sq2u_quant.hpp:39-52: dim j -> bits 2*(j%4) of byte j/4 */
+        for (int j = 0; j < d; ++j) out[j / 4] |= (uint8_t)(affine_code(x[j], p[0], p[1], 3) << (2 * (j & 3)));
     } else if (kind == GO_E5M2) {
         for (int j = 0; j < d; ++j) out[j] = e5m2_encode(x[j]);
     } else if (kind == GO_FP16) {
@@ -248,7 +252,7 @@ void go_encode(int kind, int metric, const float *p, const float *data, int64_t 
 int go_encode_query(int kind, int metric, const float *p, const float *q, int d, void *out) {
     int dalign, csize;
     go_layout(kind, d, &dalign, &csize);
-    if (kind == GO_SQ8U || kind == GO_SQ4U) {
+    if (kind == GO_SQ8U || kind == GO_SQ4U || kind == GO_SQ2U) {
         encode_row(kind, metric, p, q, d, csize, d, (uint8_t *)out);
         return csize;
     }
@@ -288,6 +292,15 @@ double go_distance(int kind, int metric, const void *qenc, const uint8_t *code, 
         }
         for (int i = 0; i < dalign; ++i) s += (int32_t)x[i] * (int32_t)y[i];   /* dot_s8_s8_ref */
         return (double)(-s);
+    }
+    if (kind == GO_SQ2U) {                            /* l2a_u2_u2 (x86/l2_impl.hpp:301-333): L2 on 2-bit codes, both metrics */
+        const uint8_t *x = (const uint8_t *)qenc, *y = code;
+        int32_t s = 0;
+        for (int i = 0; i < dalign; ++i) {
+            int32_t a = (x[i / 4] >> ((i & 3) * 2)) & 3, b = (y[i / 4] >> ((i & 3) * 2)) & 3;
+            s += (a - b) * (a - b);
+        }
+        return (double)s;
     }
     if (kind == GO_SQ4U) {                            /* l2_u4_u4_ref (ref/l2_ref.hpp:67-77); L2 for both metrics */
         const uint8_t *x = (const uint8_t *)qenc, *y = code;

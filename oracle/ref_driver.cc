@@ -38,6 +38,10 @@ int with_quant(const std::string &quant, const std::string &metric, int d, Fn &&
         if (l2) { glass::SQ8QuantizerUniform<Metric::L2> q(d); return fn(q); }
         glass::SQ8QuantizerUniform<Metric::IP> q(d); return fn(q);
     }
+    if (quant == "SQ2U") {
+        if (l2) { glass::SQ2QuantizerUniform<Metric::L2> q(d); return fn(q); }
+        glass::SQ2QuantizerUniform<Metric::IP> q(d); return fn(q);
+    }
     if (quant == "SQ4U") {
         if (l2) { glass::SQ4QuantizerUniform<Metric::L2> q(d); return fn(q); }
         glass::SQ4QuantizerUniform<Metric::IP> q(d); return fn(q);
