@@ -73,9 +73,10 @@ namespace {
 
 // quantizer_map (glass/quant/quant.hpp:25-43); operator[] on an unknown key yields FP32.
 int parse_quant(const std::string &q, int *kind) {
-    static const char *unsupported[] = {"SQ8", "SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "SQ2U", "PQ8"};
+    static const char *unsupported[] = {"SQ8", "SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "PQ8"};
     if (q == "SQ8U") *kind = K_SQ8U;
     else if (q == "SQ4U") *kind = K_SQ4U;
+    else if (q == "SQ2U") *kind = K_SQ2U;
     else if (q == "E5M2") *kind = K_E5M2;
     else if (q == "FP16") *kind = K_FP16;
     else if (q == "BF16") *kind = K_BF16;
@@ -91,6 +92,7 @@ int layout(int kind, int d, int *dalign, int *csize) {
     int align = 16, nbits = 32;
     if (kind == K_SQ8U) { align = 64; nbits = 8; }
     else if (kind == K_SQ4U) { align = 128; nbits = 4; }
+    else if (kind == K_SQ2U) { align = 256; nbits = 2; }  // sq2u_quant.hpp:11
     else if (kind == K_E5M2) { align = 16; nbits = 8; }
     // fp16_quant.hpp:10-16, bf16_quant.hpp:9-15: align 16 unless built with AVX512-FP16/BF16 macros that
     // the reference's build never defines
@@ -129,7 +131,7 @@ int device_kth2(const float *x, int64_t n, int64_t r0, int64_t r1, unsigned *scr
 // smallest and top-th largest.
 int calibrate(int kind, int metric, const float *x, int64_t n, int d, float *p, DevBuf &scratch, cudaStream_t st) {
     p[0] = p[1] = 0.0f;
-    if (kind != K_SQ8U && kind != K_SQ4U) return GSX_OK;
+    if (kind != K_SQ8U && kind != K_SQ4U && kind != K_SQ2U) return GSX_OK;
     int rc = scratch.ensure(512 * sizeof(unsigned));
     if (rc) return rc;
     unsigned *w = scratch.as<unsigned>();
@@ -150,7 +152,8 @@ int calibrate(int kind, int metric, const float *x, int64_t n, int d, float *p, 
     }
     int64_t nitems = (int64_t)((float)(n * (int64_t)d) * 0.1f);
     if (nitems < 1) nitems = 1;
-    int64_t top = (int64_t)((float)nitems * 0.01f) + 1;
+    // find_minmax's drop ratio: 1% for SQ4U, 5% for SQ2U (sq2u_quant.hpp:16-29)
+    int64_t top = (int64_t)((float)nitems * (kind == K_SQ2U ? 0.05f : 0.01f)) + 1;
     if (top > nitems) top = nitems;
     float mn = 0.0f, mx = 0.0f;
     if ((rc = device_kth2(x, nitems, top - 1, nitems - top, w, st, &mn, &mx))) return rc;
@@ -583,9 +586,9 @@ int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quanti
     int rc = parse_quant(quantizer ? quantizer : "", &kind);
     if (rc) return rc;
     const std::string rq = refine_quant ? refine_quant : "";
-    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ4U, 1.0 otherwise (in which
+    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ4U, 3 for SQ2U, 1.0 otherwise (in which
     // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
-    const float factor = (kind == K_SQ8U || kind == K_SQ4U) ? 1.5f : 1.0f;
+    const float factor = kind == K_SQ2U ? 3.0f : (kind == K_SQ8U || kind == K_SQ4U) ? 1.5f : 1.0f;
     // make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer map
     // does not know -> FP32 store; SQ8U / SQ8 -> their own refiners; any other known name -> none
     int rkind = K_FP32;

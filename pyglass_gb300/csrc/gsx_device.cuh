@@ -29,7 +29,7 @@ __device__ __forceinline__ float dist_of_key_float(uint32_t k) {
 
 template <int KIND>
 struct IsIntKind {
-    static constexpr bool value = (KIND == K_SQ8U || KIND == K_SQ4U);
+    static constexpr bool value = (KIND == K_SQ8U || KIND == K_SQ4U || KIND == K_SQ2U);
 };
 
 // ---- query encoding ---------------------------------------------------------------------------
@@ -54,7 +54,15 @@ __device__ __forceinline__ int sym_code(float x, float mx, float mul) {
 // Code byte `b` of an encoded row (base or query) for the SQ kinds; x = fp32 row, zero past d.
 template <int KIND, int METRIC>
 __device__ __forceinline__ uint32_t sq_code_byte(const float *x, int d, int b, float p0, float p1) {
-    if (KIND == K_SQ4U) {  // sq4u_quant.hpp:319-329: even dim -> low nibble
+    if (KIND == K_SQ2U) {  // sq2u_quant.hpp:39-52: dim 4b+k -> bits 2k of byte b
+        uint32_t byte = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int j = 4 * b + k;
+            if (j < d) byte |= (uint32_t)affine_code(x[j], p0, p1, 3.0f) << (2 * k);
+        }
+        return byte;
+    } else if (KIND == K_SQ4U) {  // sq4u_quant.hpp:319-329: even dim -> low nibble
         int j0 = 2 * b, j1 = 2 * b + 1;
         uint32_t lo = j0 < d ? (uint32_t)affine_code(x[j0], p0, p1, 15.0f) : 0u;
         uint32_t hi = j1 < d ? (uint32_t)affine_code(x[j1], p0, p1, 15.0f) : 0u;
@@ -91,6 +99,18 @@ __device__ __forceinline__ int32_t team_sum(int32_t v) {
 //   SQ4U: words [0, nw) = low nibbles of the query code (0x0F0F0F0F lanes), [nw, 2nw) = high
 //         nibbles; nw = csize/4.  Sum of squares of all nibbles in qsq.
 //   SQ8U: words [0, nw) = the code bytes.  L2 also uses qsq.
+//   SQ2U: words [k*nw, (k+1)*nw), k = 0..3 = the query's 2-bit codes at bits 2k of each byte, one per
+//         byte (0x03030303 lanes); qsq as for SQ4U.
+// SQ2U word: the four 2-bit planes against the query's planes (l2a_u2_u2, helpa x86/l2_impl.hpp:301-333).
+__device__ __forceinline__ void sq2_word(uint32_t w, const uint32_t *qp, int nw, uint32_t &aa, uint32_t &ab) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t x = (w >> (2 * k)) & 0x03030303u;
+        aa = __dp4a(x, x, aa);
+        ab = __dp4a(x, qp[k * nw], ab);
+    }
+}
+
 __device__ __forceinline__ void sq4_word(uint32_t w, uint32_t ql, uint32_t qh, uint32_t &aa, uint32_t &ab) {
     uint32_t lo = w & 0x0F0F0F0Fu, hi = (w >> 4) & 0x0F0F0F0Fu;
     aa = __dp4a(lo, lo, aa);
@@ -104,7 +124,20 @@ __device__ __forceinline__ int32_t sq_partial(const uint8_t *__restrict__ codes,
                                              const uint32_t *qc) {
     const uint4 *row = reinterpret_cast<const uint4 *>(codes + (size_t)id * (size_t)csize);
     const int nch = csize >> 4;
-    if (KIND == K_SQ4U) {
+    if (KIND == K_SQ2U) {
+        const int nw = csize >> 2;
+        uint32_t aa = 0, ab = 0;
+#pragma unroll 2
+        for (int c = sub; c < nch; c += LPR) {
+            const uint4 v = __ldg(row + c);
+            const uint32_t *q = qc + 4 * c;
+            sq2_word(v.x, q + 0, nw, aa, ab);
+            sq2_word(v.y, q + 1, nw, aa, ab);
+            sq2_word(v.z, q + 2, nw, aa, ab);
+            sq2_word(v.w, q + 3, nw, aa, ab);
+        }
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (KIND == K_SQ4U) {
         const uint4 *ql = reinterpret_cast<const uint4 *>(qc);
         const uint4 *qh = reinterpret_cast<const uint4 *>(qc + (csize >> 2));
         uint32_t aa = 0, ab = 0;
@@ -151,7 +184,20 @@ __device__ __forceinline__ int32_t sq_partial(const uint8_t *__restrict__ codes,
 // arithmetic as sq_partial with one lane.
 template <int KIND, int METRIC>
 __device__ __forceinline__ int32_t sq_partial_row(const uint4 *row, int nch, const uint32_t *qc) {
-    if (KIND == K_SQ4U) {
+    if (KIND == K_SQ2U) {
+        const int nw = 4 * nch;
+        uint32_t aa = 0, ab = 0;
+#pragma unroll 2
+        for (int c = 0; c < nch; ++c) {
+            const uint4 v = row[c];
+            const uint32_t *q = qc + 4 * c;
+            sq2_word(v.x, q + 0, nw, aa, ab);
+            sq2_word(v.y, q + 1, nw, aa, ab);
+            sq2_word(v.z, q + 2, nw, aa, ab);
+            sq2_word(v.w, q + 3, nw, aa, ab);
+        }
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (KIND == K_SQ4U) {
         const uint4 *ql = reinterpret_cast<const uint4 *>(qc);
         const uint4 *qh = reinterpret_cast<const uint4 *>(qc + 4 * nch);
         uint32_t aa = 0, ab = 0;

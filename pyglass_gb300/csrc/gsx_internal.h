@@ -8,7 +8,7 @@
 namespace gsx {
 
 // Quantizer kinds and metrics (values follow glass/quant/quant.hpp:25-43 and glass/common.hpp).
-enum Kind : int { K_FP32 = 0, K_FP16 = 1, K_BF16 = 2, K_E5M2 = 3, K_SQ8U = 4, K_SQ4U = 7 };
+enum Kind : int { K_FP32 = 0, K_FP16 = 1, K_BF16 = 2, K_E5M2 = 3, K_SQ8U = 4, K_SQ4U = 7, K_SQ2U = 11 };
 
 // Kinds whose codes decode to floats compared against the fp32 query (the float engines).
 inline bool is_float_kind(int k) { return k == K_FP32 || k == K_FP16 || k == K_BF16 || k == K_E5M2; }

@@ -483,7 +483,14 @@ __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState 
 #pragma unroll
         for (int t = 0; t < 4; ++t)
             word |= sq_code_byte<KIND, METRIC>(w.fq, ix.d, 4 * wi + t, ix.p0, ix.p1) << (8 * t);
-        if (KIND == K_SQ4U) {
+        if (KIND == K_SQ2U) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t x = (word >> (2 * k)) & 0x03030303u;
+                w.qc[k * nw + wi] = x;
+                sq = __dp4a(x, x, (uint32_t)sq);
+            }
+        } else if (KIND == K_SQ4U) {
             uint32_t lo = word & 0x0F0F0F0Fu, hi = (word >> 4) & 0x0F0F0F0Fu;
             w.qc[wi] = lo;
             w.qc[nw + wi] = hi;
@@ -913,6 +920,10 @@ template <template <int, int, int> class F, typename... A>
 auto dispatch(int kind, int metric, int lpr, A &&...a) {
     const bool ip = metric == M_IP;
     switch (kind) {
+        case K_SQ2U:  // L2 on codes for both metrics (sq2u_quant.hpp:55)
+            if (lpr >= 4) return F<K_SQ2U, M_L2, 4>::run(a...);
+            if (lpr == 2) return F<K_SQ2U, M_L2, 2>::run(a...);
+            return F<K_SQ2U, M_L2, 1>::run(a...);
         case K_SQ4U:  // L2 on codes for both metrics (sq4u_quant.hpp:343)
             if (lpr >= 4) return F<K_SQ4U, M_L2, 4>::run(a...);
             if (lpr == 2) return F<K_SQ4U, M_L2, 2>::run(a...);
@@ -987,13 +998,14 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     L->fq_len = fq;
     L->qc = off;
     if (ix.kind == K_SQ4U) off += up(2 * ix.csize, 16);
+    else if (ix.kind == K_SQ2U) off += up(4 * ix.csize, 16);
     else if (ix.kind == K_SQ8U) off += up(ix.csize, 16);
     L->table = off;
     if (table_bits > 0) off += (1 << table_bits) * 4;
     off = up(off, 16);
     L->stage = off;
     L->stage_row = 0;
-    if ((ix.kind == K_SQ4U || ix.kind == K_SQ8U) && !(prefetch & kNoStageCodes) && ix.csize <= 128 &&
+    if ((ix.kind == K_SQ4U || ix.kind == K_SQ8U || ix.kind == K_SQ2U) && !(prefetch & kNoStageCodes) && ix.csize <= 128 &&
         ix.csize % 16 == 0) {
         L->stage_row = ix.csize;
         off += 32 * ix.csize;
