@@ -24,6 +24,7 @@ int go_layout(int kind, int d, int *dalign, int *csize) {
         case GO_SQ8U: align = 64; nbits = 8; break;   /* sq8u_quant.hpp:14  Quantizer<metric,64,8> */
         case GO_SQ4U: align = 128; nbits = 4; break;  /* sq4u_quant.hpp:13  Quantizer<metric,128,4> */
         case GO_SQ2U: align = 256; nbits = 2; break;  /* sq2u_quant.hpp:11  Quantizer<metric,256,2> */
+        case GO_SQ8: align = 16; nbits = 8; break;    /* sq8_quant.hpp:15-16 Quantizer<metric,16,8> */
         case GO_E5M2: align = 16; nbits = 8; break;   /* e5m2_quant.hpp:11  Quantizer<metric,16,8> */
         case GO_FP16: align = 16; nbits = 16; break;  /* fp16_quant.hpp:10-16 (no AVX512-FP16 build macro) */
         case GO_BF16: align = 16; nbits = 16; break;  /* bf16_quant.hpp:9-15 (no AVX512-BF16 build macro) */
@@ -93,7 +94,28 @@ static float find_absmax(const float *data, int64_t nitems) {
     return m;
 }
 
+/* SQ8's AffinePerDimCalibrator (calibrator.hpp:66-91) with drop ratio 0 (sq8_quant.hpp:22,29-33):
+ * find_minmax_perdim (quant/utils.hpp:52-70) walks the n*d floats in order and files float i under
+ * "dimension" i / n, so entry j holds the min and max of the j-th block of n consecutive floats (not
+ * of column j); the arrays are then extended with zeros to dalign.  p = mins[dalign], difs[dalign]. */
+static void train_sq8(const float *data, int64_t n, int d, float *p) {
+    int dalign, csize;
+    go_layout(GO_SQ8, d, &dalign, &csize);
+    for (int j = 0; j < 2 * dalign; ++j) p[j] = 0.0f;
+    for (int j = 0; j < d; ++j) {
+        const float *b = data + (int64_t)j * n;
+        float mn = b[0], mx = b[0];
+        for (int64_t i = 1; i < n; ++i) {
+            if (b[i] < mn) mn = b[i];
+            if (b[i] > mx) mx = b[i];
+        }
+        p[j] = mn;
+        p[dalign + j] = mx - mn;
+    }
+}
+
 void go_train(int kind, int metric, const float *data, int64_t n, int d, float *p) {
+    if (kind == GO_SQ8) { train_sq8(data, n, d, p); return; }
     p[0] = p[1] = 0.0f;
     if (kind == GO_SQ8U) {
         int64_t nitems = n * (int64_t)d;          /* sq8u_quant.hpp:240, drop_ratio 0 */
@@ -219,6 +241,9 @@ static void encode_row(int kind, int metric, const float *p, const float *x, int
             uint8_t y = (uint8_t)affine_code(x[j], p[0], p[1], 15);
             out[j / 2] |= (j & 1) ? (uint8_t)(y << 4) : y;
         }
+    } else if (kind == GO_SQ8) {                     /* sq8_quant.hpp:43-47: transform(x, j), mul 255 */
+        const int dalign = csize;
+        for (int j = 0; j < d; ++j) out[j] = (uint8_t)affine_code(x[j], p[j], p[dalign + j], 255);
     } else if (kind == GO_SQ2U) {                    /* sq2u_quant.hpp:39-52: dim j -> bits 2*(j%4) of byte j/4 */
         for (int j = 0; j < d; ++j) out[j / 4] |= (uint8_t)(affine_code(x[j], p[0], p[1], 3) << (2 * (j & 3)));
     } else if (kind == GO_E5M2) {
@@ -258,6 +283,10 @@ int go_encode_query(int kind, int metric, const float *p, const float *q, int d,
     }
     memset(out, 0, sizeof(float) * (size_t)dalign);  /* computer.hpp:56-59 (zero-filled align_alloc) */
     memcpy(out, q, sizeof(float) * (size_t)d);
+    if (kind == GO_SQ8) {                            /* the computer's extra arguments: mins, difs */
+        memcpy((float *)out + dalign, p, sizeof(float) * 2 * (size_t)dalign);
+        return (int)sizeof(float) * 3 * dalign;
+    }
     return (int)sizeof(float) * dalign;
 }
 
@@ -313,6 +342,24 @@ double go_distance(int kind, int metric, const void *qenc, const uint8_t *code, 
     }
     const float *q = (const float *)qenc;
     float acc[16] = {0};
+    if (kind == GO_SQ8) {
+        /* L2SqrSQ8_ext / IPSQ8_ext (glass/simd/avx512.hpp:40-75): y = (code + 0.5) * dif + 256 * min, in
+         * 256ths of the data scale, against 256 * x.  As the reference's -Ofast build evaluates them
+         * (checked against the compiled reference): IP takes y = fma(code + 0.5, dif, 256 * min);
+         * L2 reassociates 256x - y into fma(-(code + 0.5), dif, 256x - 256 * min).  Glass's reduction. */
+        const float *mi = q + dalign, *dif = q + 2 * dalign;
+        for (int i = 0; i < dalign; ++i) {
+            const float c5 = (float)code[i] + 0.5f;
+            if (metric == GO_L2) {
+                float t = fmaf(-c5, dif[i], q[i] * 256.0f - mi[i] * 256.0f);
+                acc[i & 15] = fmaf(t, t, acc[i & 15]);
+            } else {
+                acc[i & 15] = fmaf(q[i], fmaf(c5, dif[i], mi[i] * 256.0f), acc[i & 15]);
+            }
+        }
+        float r = reduce16_glass(acc);
+        return metric == GO_L2 ? (double)r : (double)(-r);
+    }
     if (kind == GO_E5M2) {
         for (int i = 0; i < dalign; ++i) {
             float y = e5m2_decode(code[i]);
@@ -448,7 +495,7 @@ static inline int pool_has_next(const pool_t *p) { return p->cur < p->size && p-
 
 typedef struct {
     const go_index *ix;
-    uint8_t qenc[1 << 14];
+    uint8_t qenc[1 << 16];
     int64_t cmps;
 } computer_t;
 
@@ -554,7 +601,7 @@ void go_search(const go_index *ix, const float *queries, int64_t nq, int k, int 
             int cap = kin > efq ? kin : efq;
             /* SearchBatch resets the pool with (ef, max(k,ef)); Search with (max(k,ef), max(k,ef)) */
             int ef_expand = single ? cap : efq;
-            go_encode_query(ix->kind, ix->metric, ix->p, q, ix->d, c->qenc);
+            go_encode_query(ix->kind, ix->metric, ix->kind == GO_SQ8 ? ix->pp : ix->p, q, ix->d, c->qenc);
             c->cmps = 0;
             pool_reset(&p, ef_expand, cap);
             initialize_search(g, &p, c);
@@ -602,7 +649,7 @@ void go_query_distances(int kind, int metric, const float *p, int d, const float
     go_layout(kind, d, &dalign, &csize);
 #pragma omp parallel
     {
-        uint8_t *qenc = (uint8_t *)malloc((size_t)dalign * 4 + 64);
+        uint8_t *qenc = (uint8_t *)malloc((size_t)dalign * 12 + 64);
 #pragma omp for schedule(static)
         for (int64_t qi = 0; qi < nq; ++qi) {
             go_encode_query(kind, metric, p, queries + qi * d, d, qenc);

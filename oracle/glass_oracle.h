@@ -20,7 +20,7 @@ extern "C" {
 #endif
 
 /* Quantizer kinds (names follow glass/quant/quant.hpp:25-43). */
-enum { GO_FP32 = 0, GO_FP16 = 1, GO_BF16 = 2, GO_E5M2 = 3, GO_SQ8U = 4, GO_SQ4U = 7, GO_SQ2U = 11 };
+enum { GO_FP32 = 0, GO_FP16 = 1, GO_BF16 = 2, GO_E5M2 = 3, GO_SQ8U = 4, GO_SQ8 = 5, GO_SQ4U = 7, GO_SQ2U = 11 };
 /* Metrics (glass/common.hpp:13-19). */
 enum { GO_L2 = 0, GO_IP = 1 };
 
@@ -78,6 +78,7 @@ typedef struct {
     int r_dalign;
     const void *r_codes;    /* N*r_dalign rows of the refine quantizer: fp32, or fp16 when r_kind = GO_FP16 */
     int r_kind;             /* GO_FP32 or GO_FP16 (make_refiner, graph_searcher.hpp:240-254) */
+    const float *pp;        /* SQ8: the calibrator's 2*dalign parameters (mins, then difs) */
 } go_index;
 
 /*

@@ -22,10 +22,10 @@ ORACLE_SO = os.path.join(HERE, "_build", "libglass_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libglass_ref.so")
 REFERENCE_DIR = os.environ.get("GLASS_REFERENCE_DIR", "/root/reference")
 
-KIND = {"FP32": 0, "FP16": 1, "BF16": 2, "E5M2": 3, "SQ8U": 4, "SQ4U": 7, "SQ2U": 11}
+KIND = {"FP32": 0, "FP16": 1, "BF16": 2, "E5M2": 3, "SQ8U": 4, "SQ8": 5, "SQ4U": 7, "SQ2U": 11}
 METRIC = {"L2": 0, "IP": 1}
 # get_refine_factor (glass/searcher/graph_searcher.hpp:227-238) for the quantizers in scope
-REFINE_FACTOR = {"SQ8U": 1.5, "SQ4U": 1.5, "SQ2U": 3.0, "E5M2": 1.0, "FP32": 1.0, "FP16": 1.0, "BF16": 1.0}
+REFINE_FACTOR = {"SQ8U": 1.5, "SQ8": 1.5, "SQ4U": 1.5, "SQ2U": 3.0, "E5M2": 1.0, "FP32": 1.0, "FP16": 1.0, "BF16": 1.0}
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -61,7 +61,7 @@ class _GoIndex(C.Structure):
         ("g", C.POINTER(_GoGraph)), ("kind", C.c_int), ("metric", C.c_int), ("d", C.c_int),
         ("dalign", C.c_int), ("csize", C.c_int), ("p", C.c_float * 2), ("codes", C.c_void_p),
         ("has_refine", C.c_int), ("refine_factor", C.c_float), ("r_dalign", C.c_int), ("r_codes", C.c_void_p),
-        ("r_kind", C.c_int),
+        ("r_kind", C.c_int), ("pp", C.c_void_p),
     ]
 
 
@@ -105,14 +105,14 @@ class Quant:
         self.kind, self.m = KIND[quant], METRIC[metric]
         self.n, self.d = data.shape
         self.dalign, self.csize = layout(quant, self.d)
-        self.params = np.zeros(2, np.float32)
+        self.params = np.zeros(2 * self.dalign if quant == "SQ8" else 2, np.float32)
         lib.go_train(self.kind, self.m, data, self.n, self.d, self.params)
         self.codes = np.zeros((self.n, self.csize), np.uint8)
         lib.go_encode(self.kind, self.m, self.params, data, self.n, self.d, self.codes)
 
     def encode_queries(self, q: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.d)
-        width = self.csize if self.quant in ("SQ8U", "SQ4U", "SQ2U") else 4 * self.dalign
+        width = self.csize if self.quant in ("SQ8U", "SQ4U", "SQ2U") else (12 if self.quant == "SQ8" else 4) * self.dalign
         out = np.zeros((q.shape[0], width), np.uint8)
         for i in range(q.shape[0]):
             _oracle_lib().go_encode_query(self.kind, self.m, self.params, q[i], self.d, out[i].ctypes.data)
@@ -157,6 +157,7 @@ class Searcher:
         self._ix.dalign, self._ix.csize = self.q.dalign, self.q.csize
         self._ix.p[0], self._ix.p[1] = float(self.q.params[0]), float(self.q.params[1])
         self._ix.codes = self.q.codes.ctypes.data
+        self._ix.pp = self.q.params.ctypes.data
         self.refine = None
         # make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer
         # map does not know -> FP32 store; any other known quantizer name -> no refiner
@@ -249,7 +250,7 @@ class RefGlass:
         lib = _ref_lib()
         cs = lib.ref_code_size(quant.encode(), metric.encode(), data.shape[1])
         codes = np.zeros((data.shape[0], cs), np.uint8)
-        params = np.zeros(2, np.float32)
+        params = np.zeros(2 * layout(quant, data.shape[1])[0] if quant == "SQ8" else 2, np.float32)
         lib.ref_encode(quant.encode(), metric.encode(), data, data.shape[0], data.shape[1], codes, params)
         return codes, params
 

@@ -38,6 +38,10 @@ int with_quant(const std::string &quant, const std::string &metric, int d, Fn &&
         if (l2) { glass::SQ8QuantizerUniform<Metric::L2> q(d); return fn(q); }
         glass::SQ8QuantizerUniform<Metric::IP> q(d); return fn(q);
     }
+    if (quant == "SQ8") {
+        if (l2) { glass::SQ8Quantizer<Metric::L2> q(d); return fn(q); }
+        glass::SQ8Quantizer<Metric::IP> q(d); return fn(q);
+    }
     if (quant == "SQ2U") {
         if (l2) { glass::SQ2QuantizerUniform<Metric::L2> q(d); return fn(q); }
         glass::SQ2QuantizerUniform<Metric::IP> q(d); return fn(q);
@@ -73,6 +77,10 @@ void calib_params(const Q &q, float *params) {
         params[1] = q.calibrator.dif;
     } else if constexpr (requires { q.calibrator.max; }) {
         params[0] = q.calibrator.max;
+    } else if constexpr (requires { q.calibrator.difs; }) {  // per-dimension: mins, then difs (dalign each)
+        const size_t n = q.calibrator.mins.size();
+        std::memcpy(params, q.calibrator.mins.data(), n * sizeof(float));
+        std::memcpy(params + n, q.calibrator.difs.data(), n * sizeof(float));
     }
 }
 

@@ -9,14 +9,15 @@ NQ_DIST, NQ_SEARCH = 16, 60
 GRAPHS = {"hnsw_d100": ("HNSW", 16, 40), "nsg_d100": ("NSG", 16, 40)}
 QUANTS = [("SQ8U", "L2"), ("SQ8U", "IP"), ("SQ4U", "L2"), ("SQ4U", "IP"), ("E5M2", "L2"), ("E5M2", "IP"),
           ("FP32", "L2"), ("FP32", "IP"), ("FP16", "L2"), ("FP16", "IP"), ("BF16", "L2"), ("BF16", "IP"),
-          ("SQ2U", "L2"), ("SQ2U", "IP")]
+          ("SQ2U", "L2"), ("SQ2U", "IP"), ("SQ8", "L2"), ("SQ8", "IP")]
 # (quant, metric, refine)
 SEARCHERS = [("SQ8U", "L2", ""), ("SQ8U", "IP", ""), ("SQ4U", "L2", "FP32"), ("SQ4U", "IP", "FP32"),
              ("E5M2", "L2", ""), ("E5M2", "IP", ""), ("FP32", "L2", ""), ("FP32", "IP", ""), ("SQ8U", "L2", "FP32"),
              ("FP16", "L2", ""), ("FP16", "IP", ""), ("BF16", "L2", ""), ("BF16", "IP", ""),
              # make_refiner: an FP16 store; a known quantizer without a refiner; a name the map lacks (FP32)
              ("SQ4U", "L2", "FP16"), ("SQ8U", "IP", "FP16"), ("SQ4U", "L2", "BF16"), ("SQ4U", "IP", "FP64"),
-             ("SQ2U", "L2", ""), ("SQ2U", "L2", "FP32"), ("SQ2U", "IP", "FP32")]
+             ("SQ2U", "L2", ""), ("SQ2U", "L2", "FP32"), ("SQ2U", "IP", "FP32"),
+             ("SQ8", "L2", ""), ("SQ8", "IP", ""), ("SQ8", "L2", "FP32")]
 # (ef, k): includes k > ef, the case where search and batch_search differ (graph_searcher.hpp:134,152)
 EFK = [(16, 10), (40, 10), (8, 20)]
 
