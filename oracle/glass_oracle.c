@@ -344,14 +344,15 @@ double go_distance(int kind, int metric, const void *qenc, const uint8_t *code, 
     float acc[16] = {0};
     if (kind == GO_SQ8) {
         /* L2SqrSQ8_ext / IPSQ8_ext (glass/simd/avx512.hpp:40-75): y = (code + 0.5) * dif + 256 * min, in
-         * 256ths of the data scale, against 256 * x.  As the reference's -Ofast build evaluates them
-         * (checked against the compiled reference): IP takes y = fma(code + 0.5, dif, 256 * min);
-         * L2 reassociates 256x - y into fma(-(code + 0.5), dif, 256x - 256 * min).  Glass's reduction. */
+         * 256ths of the data scale, against 256 * x, with y = fma(code + 0.5, dif, 256 * min): the
+         * contraction the reference's -Ofast build applies inside its search loop (checked against the
+         * compiled reference's search results).  A stand-alone compiled copy of the L2 kernel
+         * reassociates 256x - y differently and lands 1-2 ulp away.  Glass's reduction. */
         const float *mi = q + dalign, *dif = q + 2 * dalign;
         for (int i = 0; i < dalign; ++i) {
             const float c5 = (float)code[i] + 0.5f;
             if (metric == GO_L2) {
-                float t = fmaf(-c5, dif[i], q[i] * 256.0f - mi[i] * 256.0f);
+                float t = q[i] * 256.0f - fmaf(c5, dif[i], mi[i] * 256.0f);
                 acc[i & 15] = fmaf(t, t, acc[i & 15]);
             } else {
                 acc[i & 15] = fmaf(q[i], fmaf(c5, dif[i], mi[i] * 256.0f), acc[i & 15]);

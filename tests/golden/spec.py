@@ -30,6 +30,13 @@ def queries():
     return datasets.gaussian(NQ_SEARCH, D, seed=11, stream=1)
 
 
+# Float kernels whose rounding the reference's -Ofast build varies between its compiled copies (the
+# batch loop, the single-query loop, the stand-alone computer differ by 1-2 ulp): their distances are
+# checked to the floating-point tolerance (relative 1e-5); ids and distance counts stay exact.
+FLOAT_TOLERANT = {("SQ8", "L2")}
+RTOL = 1e-5
+
+
 def search_cases():
     for g, (q, m, r), (ef, k), mode in itertools.product(GRAPHS, SEARCHERS, EFK, ["batch", "single"]):
         if mode == "single" and ef != 8:

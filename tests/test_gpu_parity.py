@@ -45,7 +45,10 @@ def test_distances_bit_exact(gpu, golden, quant, metric):
     s = searcher(gpu, "nsg_d100", quant, metric, refine)
     q = spec.queries()[: spec.NQ_DIST]
     d = s.distances(q, golden["dist_ids"])
-    np.testing.assert_array_equal(d, golden[f"dist/{quant}/{metric}"])
+    if (quant, metric) in spec.FLOAT_TOLERANT:
+        np.testing.assert_allclose(d, golden[f"dist/{quant}/{metric}"], rtol=spec.RTOL, atol=0)
+    else:
+        np.testing.assert_array_equal(d, golden[f"dist/{quant}/{metric}"])
     if refine:
         d = s.distances(q, golden["dist_ids"], refine=True)
         np.testing.assert_array_equal(d, golden[f"dist/FP32/{metric}"])
@@ -65,7 +68,10 @@ def test_search_matches_reference(gpu, golden, case):
         res = [s.search(q[i], k) for i in range(q.shape[0])]
         ids, dis = np.stack([r[0] for r in res]), np.stack([r[1] for r in res])
     np.testing.assert_array_equal(ids, golden[f"ids/{key}"])
-    np.testing.assert_array_equal(dis, golden[f"dis/{key}"])
+    if (quant, metric) in spec.FLOAT_TOLERANT:
+        np.testing.assert_allclose(dis, golden[f"dis/{key}"], rtol=spec.RTOL, atol=0)
+    else:
+        np.testing.assert_array_equal(dis, golden[f"dis/{key}"])
 
 
 @pytest.mark.parametrize("K", [5, 32, 48])

@@ -18,7 +18,10 @@ def test_codes_params_distances(oracle, golden, quant, metric):
     assert hashlib.sha256(qz.codes.tobytes()).digest() == golden[f"codes_sha/{quant}/{metric}"].tobytes()
     np.testing.assert_array_equal(qz.params, golden[f"params/{quant}/{metric}"])
     d = qz.distances(q, golden["dist_ids"])
-    np.testing.assert_array_equal(d, golden[f"dist/{quant}/{metric}"])  # bit-exact, floats included
+    if (quant, metric) in spec.FLOAT_TOLERANT:
+        np.testing.assert_allclose(d, golden[f"dist/{quant}/{metric}"], rtol=spec.RTOL, atol=0)
+    else:
+        np.testing.assert_array_equal(d, golden[f"dist/{quant}/{metric}"])  # bit-exact, floats included
 
 
 @pytest.mark.parametrize("case", list(spec.search_cases()), ids=spec.case_key)
@@ -36,4 +39,7 @@ def test_search(oracle, golden, case):
         res = [s.search(q[i], k) for i in range(q.shape[0])]
         ids, dis = np.stack([r[0] for r in res]), np.stack([r[1] for r in res])
     np.testing.assert_array_equal(ids, golden[f"ids/{key}"])
-    np.testing.assert_array_equal(dis, golden[f"dis/{key}"])
+    if (quant, metric) in spec.FLOAT_TOLERANT:
+        np.testing.assert_allclose(dis, golden[f"dis/{key}"], rtol=spec.RTOL, atol=0)
+    else:
+        np.testing.assert_array_equal(dis, golden[f"dis/{key}"])
