@@ -170,8 +170,14 @@ int gsx_searcher_memory(const gsx_searcher *s, size_t *index_bytes, size_t *per_
 int gsx_searcher_distances(gsx_searcher *s, const float *queries, int32_t nq, const int32_t *ids, int32_t m,
                            int32_t refine, double *out);
 
-/* Copies out the encoded base rows (n*code_size bytes) and calibrator parameters (2 floats). */
+/* Copies out the encoded base rows (n*code_size bytes) and calibrator parameters (2 floats: min and
+ * dif, or max for the symmetric calibrator; for SQ8 the first dimension's min and dif, see below). */
 int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int32_t *code_size);
+
+/* All calibrator parameters of the search quantizer: *count = 2 (scalar calibrators), or 2*dalign for
+ * SQ8's per-dimension calibrator (AffinePerDimCalibrator, calibrator.hpp:66-91: mins then difs).
+ * params may be NULL to ask for the count. */
+int gsx_searcher_params(const gsx_searcher *s, float *params, int32_t *count);
 
 /* ---- exact ground truth (no reference counterpart; replaces brute force in examples/main.py) -- */
 

@@ -69,7 +69,54 @@ __global__ void radix_hist2(const float *__restrict__ x, int64_t n, uint2 prefix
     }
 }
 
+// SQ8's AffinePerDimCalibrator (calibrator.hpp:66-91) with drop ratio 0: find_minmax_perdim
+// (quant/utils.hpp:52-70) files float i of the row-major data under "dimension" i / n, so entry j
+// is the min / max of the j-th block of n consecutive floats.  One block of threads per entry.
+__global__ void block_minmax(const float *__restrict__ x, int64_t n, int d, int dalign, float *__restrict__ out) {
+    const int j = blockIdx.x;
+    if (j >= dalign) return;
+    if (j >= d) {
+        if (threadIdx.x == 0) out[j] = out[dalign + j] = 0.0f;
+        return;
+    }
+    const float *b = x + (int64_t)j * n;
+    uint32_t mn = 0xffffffffu, mx = 0u;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t k = fkey(b[i]);
+        mn = k < mn ? k : mn;
+        mx = k > mx ? k : mx;
+    }
+    __shared__ uint32_t smn[32], smx[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t a = __shfl_xor_sync(0xffffffffu, mn, o), c = __shfl_xor_sync(0xffffffffu, mx, o);
+        mn = a < mn ? a : mn;
+        mx = c > mx ? c : mx;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        smn[threadIdx.x >> 5] = mn;
+        smx[threadIdx.x >> 5] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            mn = smn[w] < mn ? smn[w] : mn;
+            mx = smx[w] > mx ? smx[w] : mx;
+        }
+        const uint32_t umn = (mn & 0x80000000u) ? (mn & 0x7fffffffu) : ~mn;
+        const uint32_t umx = (mx & 0x80000000u) ? (mx & 0x7fffffffu) : ~mx;
+        const float fmn = __uint_as_float(umn), fmx = __uint_as_float(umx);
+        out[j] = fmn;
+        out[dalign + j] = fmx - fmn;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_block_minmax(const float *x, int64_t n, int d, int dalign, float *out, cudaStream_t st) {
+    block_minmax<<<dalign, kThreads, 0, st>>>(x, n, d, dalign, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_minmax_keys(const float *x, int64_t n, int absval, unsigned *out, cudaStream_t st) {
     const unsigned init[2] = {0xffffffffu, 0u};

@@ -67,6 +67,18 @@ __global__ void encode_half_rows(const float *__restrict__ data, int64_t n, int 
     }
 }
 
+// SQ8 rows (sq8_quant.hpp:43-47): code = transform(x, j) with the per-dimension calibrator, mul 255;
+// the padding stays zero.  p = mins[dalign] then difs[dalign].
+__global__ void encode_sq8_rows(const float *__restrict__ data, int64_t n, int d, int dalign,
+                                const float *__restrict__ p, uint8_t *__restrict__ out) {
+    const int64_t total = n * (int64_t)dalign;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = t / dalign;
+        const int j = (int)(t - row * dalign);
+        out[t] = j < d ? (uint8_t)affine_code(data[row * (int64_t)d + j], p[j], p[dalign + j], 255.0f) : (uint8_t)0;
+    }
+}
+
 __global__ void pad_rows(const float *__restrict__ data, int64_t n, int d, int dalign, float *__restrict__ out) {
     const int64_t total = n * (int64_t)dalign;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -97,6 +109,12 @@ cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, in
     else if (kind == K_FP16) encode_half_rows<K_FP16><<<g, 256, 0, st>>>(data, n, d, dalign, o);
     else if (kind == K_BF16) encode_half_rows<K_BF16><<<g, 256, 0, st>>>(data, n, d, dalign, o);
     else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_encode_sq8(const float *data, int64_t n, int d, int dalign, const float *p, uint8_t *out,
+                              cudaStream_t st) {
+    encode_sq8_rows<<<grid_for(n * dalign), 256, 0, st>>>(data, n, d, dalign, p, out);
     return cudaGetLastError();
 }
 

@@ -73,10 +73,11 @@ namespace {
 
 // quantizer_map (glass/quant/quant.hpp:25-43); operator[] on an unknown key yields FP32.
 int parse_quant(const std::string &q, int *kind) {
-    static const char *unsupported[] = {"SQ8", "SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "PQ8"};
+    static const char *unsupported[] = {"SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "PQ8"};
     if (q == "SQ8U") *kind = K_SQ8U;
     else if (q == "SQ4U") *kind = K_SQ4U;
     else if (q == "SQ2U") *kind = K_SQ2U;
+    else if (q == "SQ8") *kind = K_SQ8;
     else if (q == "E5M2") *kind = K_E5M2;
     else if (q == "FP16") *kind = K_FP16;
     else if (q == "BF16") *kind = K_BF16;
@@ -93,6 +94,7 @@ int layout(int kind, int d, int *dalign, int *csize) {
     if (kind == K_SQ8U) { align = 64; nbits = 8; }
     else if (kind == K_SQ4U) { align = 128; nbits = 4; }
     else if (kind == K_SQ2U) { align = 256; nbits = 2; }  // sq2u_quant.hpp:11
+    else if (kind == K_SQ8) { align = 16; nbits = 8; }    // sq8_quant.hpp:15-16
     else if (kind == K_E5M2) { align = 16; nbits = 8; }
     // fp16_quant.hpp:10-16, bf16_quant.hpp:9-15: align 16 unless built with AVX512-FP16/BF16 macros that
     // the reference's build never defines
@@ -586,9 +588,9 @@ int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quanti
     int rc = parse_quant(quantizer ? quantizer : "", &kind);
     if (rc) return rc;
     const std::string rq = refine_quant ? refine_quant : "";
-    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ4U, 3 for SQ2U, 1.0 otherwise (in which
+    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ8/SQ4U, 3 for SQ2U, 1.0 otherwise (in which
     // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
-    const float factor = kind == K_SQ2U ? 3.0f : (kind == K_SQ8U || kind == K_SQ4U) ? 1.5f : 1.0f;
+    const float factor = kind == K_SQ2U ? 3.0f : (kind == K_SQ8U || kind == K_SQ4U || kind == K_SQ8) ? 1.5f : 1.0f;
     // make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer map
     // does not know -> FP32 store; SQ8U / SQ8 -> their own refiners; any other known name -> none
     int rkind = K_FP32;
@@ -657,7 +659,7 @@ void gsx_searcher_destroy(gsx_searcher *s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
-    for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->q, &s->ids,
+    for (DevBuf *b : {&s->adj, &s->eps, &s->levels, &s->loff, &s->lists, &s->codes, &s->r_codes, &s->sq8p, &s->q, &s->ids,
                       &s->dis, &s->status, &s->cmps, &s->efp, &s->kp, &s->order, &s->counters, &s->gtab.buf,
                       &s->spill.buf, &s->dist_out, &s->dist_ids, &s->pdir, &s->qkeys, &s->qorder})
         b->release();
@@ -684,8 +686,17 @@ int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t
     ix.p0 = p[0];
     ix.p1 = p[1];
     if ((rc = s->codes.ensure((size_t)n * ix.csize))) return rc;
+    ix.sq8p = nullptr;
     if (s->kind == K_FP32) {
         GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.dalign, s->codes.as<float>(), st));
+    } else if (s->kind == K_SQ8) {
+        // the per-dimension calibrator trained and applied on the device (calib_kernel.cu)
+        if ((rc = s->sq8p.ensure((size_t)2 * ix.dalign * 4))) return rc;
+        GSX_CUDA(launch_block_minmax(raw.as<float>(), n, dim, ix.dalign, s->sq8p.as<float>(), st));
+        GSX_CUDA(launch_encode_sq8(raw.as<float>(), n, dim, ix.dalign, s->sq8p.as<float>(), s->codes.as<uint8_t>(), st));
+        s->h_sq8p.resize((size_t)2 * ix.dalign);
+        GSX_CUDA(cudaMemcpyAsync(s->h_sq8p.data(), s->sq8p.p, s->h_sq8p.size() * 4, cudaMemcpyDeviceToHost, st));
+        ix.sq8p = s->sq8p.as<float>();
     } else {
         GSX_CUDA(launch_encode(s->kind, s->metric, raw.as<float>(), n, dim, ix.dalign, ix.csize, ix.p0, ix.p1,
                                s->codes.as<uint8_t>(), st));
@@ -863,7 +874,7 @@ int gsx_searcher_memory(const gsx_searcher *s, size_t *index_bytes, size_t *per_
     if (!s) return fail(GSX_ERR_INVALID, "null searcher");
     if (index_bytes)
         *index_bytes = s->adj.bytes + s->eps.bytes + s->levels.bytes + s->loff.bytes + s->lists.bytes + s->codes.bytes +
-                       s->r_codes.bytes;
+                       s->r_codes.bytes + s->sq8p.bytes;
     if (per_query_bytes) {
         // device bytes one in-flight query holds outside the resident index: its fp32 row,
         // outputs (k up to 256), status and counter
@@ -897,13 +908,30 @@ int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int
     if (!s->has_data) return fail(GSX_ERR_STATE, "codes before set_data");
     if (code_size) *code_size = s->ix.csize;
     if (params) {
-        params[0] = s->ix.p0;
-        params[1] = s->ix.p1;
+        const bool sq8 = s->kind == K_SQ8 && !s->h_sq8p.empty();
+        params[0] = sq8 ? s->h_sq8p[0] : s->ix.p0;
+        params[1] = sq8 ? s->h_sq8p[s->h_sq8p.size() / 2] : s->ix.p1;
     }
     if (codes) {
         int rc = set_device(s);
         if (rc) return rc;
         GSX_CUDA(cudaMemcpy(codes, s->codes.p, (size_t)s->ix.N * s->ix.csize, cudaMemcpyDeviceToHost));
+    }
+    return GSX_OK;
+}
+
+int gsx_searcher_params(const gsx_searcher *s, float *params, int32_t *count) {
+    if (!s || !count) return fail(GSX_ERR_INVALID, "null argument");
+    if (!s->has_data) return fail(GSX_ERR_STATE, "params before set_data");
+    if (s->kind == K_SQ8) {
+        *count = (int32_t)s->h_sq8p.size();
+        if (params) std::memcpy(params, s->h_sq8p.data(), s->h_sq8p.size() * 4);
+    } else {
+        *count = 2;
+        if (params) {
+            params[0] = s->ix.p0;
+            params[1] = s->ix.p1;
+        }
     }
     return GSX_OK;
 }

@@ -258,11 +258,13 @@ __device__ __forceinline__ int32_t sq_finish(int32_t partial, int32_t qsq) {
 // lane owns NA = 16/LPR consecutive accumulators; the first tree levels cross lanes by shuffles.
 // FP16 and BF16 codes (helpa x86 l2a/dota_fp32_fp16, _fp32_bf16: the same 16 fused accumulators and
 // helpa reduction as FP32) widen exactly to fp32 before the arithmetic.
+// SQ8 (L2SqrSQ8_ext / IPSQ8_ext, glass/simd/avx512.hpp:40-75): y = fma(code + 0.5, dif, 256 min)
+// against 256 q (L2: (256q - y)^2, IP: q*y), glass's reduction; `ext` = mins[16*nsteps] then difs.
 template <int KIND, int METRIC, int LPR>
 __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_bytes, int nsteps, int sub,
-                                            const float *fq, bool active) {
+                                            const float *fq, bool active, const float *__restrict__ ext = nullptr) {
     constexpr int NA = 16 / LPR;
-    constexpr bool E5M2 = KIND == K_E5M2;
+    constexpr bool E5M2 = KIND == K_E5M2 || KIND == K_SQ8;  // glass's reduction tree
     float a[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) a[i] = 0.0f;
@@ -288,7 +290,22 @@ __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_byte
                     if constexpr (KIND == K_FP16) y[i] = __half2float(__ushort_as_half((unsigned short)h));
                     else y[i] = __uint_as_float(h << 16);
                 }
-            } else if constexpr (E5M2) {
+            } else if constexpr (KIND == K_SQ8) {
+                static_assert(NA == 4 || NA == 16, "SQ8 engine supports 1 or 4 lanes per row");
+                uint32_t ws[NA / 4];
+                if constexpr (NA == 16) {
+                    const uint4 w = __ldg(reinterpret_cast<const uint4 *>(row_bytes + base));
+                    ws[0] = w.x; ws[1] = w.y; ws[2] = w.z; ws[3] = w.w;
+                } else {
+                    ws[0] = __ldg(reinterpret_cast<const uint32_t *>(row_bytes + base));
+                }
+                const float *mi = ext + base, *dif = ext + 16 * nsteps + base;
+#pragma unroll
+                for (int i = 0; i < NA; ++i) {
+                    const float c5 = (float)((ws[i >> 2] >> (8 * (i & 3))) & 0xffu) + 0.5f;
+                    y[i] = fmaf(c5, __ldg(dif + i), __ldg(mi + i) * 256.0f);
+                }
+            } else if constexpr (KIND == K_E5M2) {
                 if constexpr (NA == 16) {
                     uint4 w = __ldg(reinterpret_cast<const uint4 *>(row_bytes + base));
                     uint32_t ws[4] = {w.x, w.y, w.z, w.w};
@@ -316,7 +333,8 @@ __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_byte
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     if (METRIC == M_L2) {
-                        float df = qq[t] - y[4 * i + t];
+                        const float qv = KIND == K_SQ8 ? qq[t] * 256.0f : qq[t];
+                        float df = qv - y[4 * i + t];
                         a[4 * i + t] = fmaf(df, df, a[4 * i + t]);
                     } else {
                         a[4 * i + t] = fmaf(qq[t], y[4 * i + t], a[4 * i + t]);

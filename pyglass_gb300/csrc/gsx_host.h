@@ -82,7 +82,8 @@ struct gsx_searcher {
     // device index
     bool has_data = false;
     gsx::IndexView ix{};
-    gsx::DevBuf adj, eps, levels, loff, lists, codes, r_codes;
+    gsx::DevBuf adj, eps, levels, loff, lists, codes, r_codes, sq8p;
+    std::vector<float> h_sq8p;  // host copy of SQ8's per-dimension parameters (mins, then difs)
     cudaStream_t stream = nullptr;
     int num_sms = 0;
 

@@ -8,10 +8,11 @@
 namespace gsx {
 
 // Quantizer kinds and metrics (values follow glass/quant/quant.hpp:25-43 and glass/common.hpp).
-enum Kind : int { K_FP32 = 0, K_FP16 = 1, K_BF16 = 2, K_E5M2 = 3, K_SQ8U = 4, K_SQ4U = 7, K_SQ2U = 11 };
+enum Kind : int { K_FP32 = 0, K_FP16 = 1, K_BF16 = 2, K_E5M2 = 3, K_SQ8U = 4, K_SQ8 = 5, K_SQ4U = 7, K_SQ2U = 11 };
 
 // Kinds whose codes decode to floats compared against the fp32 query (the float engines).
-inline bool is_float_kind(int k) { return k == K_FP32 || k == K_FP16 || k == K_BF16 || k == K_E5M2; }
+// SQ8 (per-dimension affine codes) decodes each code to a float with its dimension's min and dif.
+inline bool is_float_kind(int k) { return k == K_FP32 || k == K_FP16 || k == K_BF16 || k == K_E5M2 || k == K_SQ8; }
 enum MetricId : int { M_L2 = 0, M_IP = 1 };
 
 constexpr int kMaxDegree = 64;       // graph degree handled per row (two 32-wide chunks)
@@ -41,6 +42,7 @@ struct IndexView {
     int32_t kind, metric, d, dalign, csize;
     float p0, p1;             // calibrator (min, dif) or (max, 0)
     const uint8_t *codes;     // N*csize
+    const float *sq8p;        // SQ8: mins[dalign] then difs[dalign] of its calibrator, else null
     int32_t has_refine;
     float refine_factor;
     int32_t r_dalign;
@@ -120,6 +122,11 @@ cudaError_t launch_minmax_keys(const float *x, int64_t n, int absval, unsigned *
 cudaError_t launch_radix_hist2(const float *x, int64_t n, uint32_t prefix0, uint32_t prefix1, uint32_t mask, int shift,
                                unsigned *hist, cudaStream_t st);
 float float_of_key(uint32_t k);
+// SQ8's calibrator: mins[j], difs[j] = min and max-min of the j-th block of n consecutive floats of x
+// (j < d; see calib_kernel.cu); entries d..dalign-1 zero.  out = mins[dalign] then difs[dalign].
+cudaError_t launch_block_minmax(const float *x, int64_t n, int d, int dalign, float *out, cudaStream_t st);
+cudaError_t launch_encode_sq8(const float *data, int64_t n, int d, int dalign, const float *p, uint8_t *out,
+                              cudaStream_t st);
 
 // Work order of a batch (order_kernel.cu): order[0..nq) = the queries sorted by the bin of their
 // projection (q - mean) . dir; dirmean = dir[d] then mean[d]; keys = nq words of scratch.

@@ -203,10 +203,15 @@ struct Searcher {
 
     // (code size in bytes, calibrator parameters) of the search quantizer
     py::tuple calibration() {
-        int32_t cs = 0;
+        int32_t cs = 0, np_ = 0;
         float p[2];
         check(gsx_searcher_codes(s, nullptr, p, &cs));
-        return py::make_tuple(cs, py::make_tuple(p[0], p[1]));
+        check(gsx_searcher_params(s, nullptr, &np_));
+        std::vector<float> v((size_t)np_);
+        check(gsx_searcher_params(s, v.data(), &np_));
+        py::tuple t((size_t)np_);
+        for (int32_t i = 0; i < np_; ++i) t[(size_t)i] = v[(size_t)i];
+        return py::make_tuple(cs, t);
     }
 
     py::array_t<uint8_t> code_rows(int n) {

@@ -415,7 +415,7 @@ __device__ __forceinline__ void compute_dists(const IndexView &ix, WarpState &w,
             key = key_of(sq_finish<KIND, METRIC, LPR>(part, qsq));
         } else {
             const uint8_t *row = ix.codes + (size_t)id * (size_t)ix.csize;
-            float dv = float_dist<KIND, METRIC, LPR>(row, ix.dalign >> 4, sub, w.fq, act);
+            float dv = float_dist<KIND, METRIC, LPR>(row, ix.dalign >> 4, sub, w.fq, act, ix.sq8p);
             key = key_of(dv);
         }
         if (act && sub == 0) w.cand_key[j] = key;
@@ -940,6 +940,9 @@ auto dispatch(int kind, int metric, int lpr, A &&...a) {
         case K_E5M2:
             if (ip) return lpr == 1 ? F<K_E5M2, M_IP, 1>::run(a...) : F<K_E5M2, M_IP, 4>::run(a...);
             return lpr == 1 ? F<K_E5M2, M_L2, 1>::run(a...) : F<K_E5M2, M_L2, 4>::run(a...);
+        case K_SQ8:
+            if (ip) return lpr == 1 ? F<K_SQ8, M_IP, 1>::run(a...) : F<K_SQ8, M_IP, 4>::run(a...);
+            return lpr == 1 ? F<K_SQ8, M_L2, 1>::run(a...) : F<K_SQ8, M_L2, 4>::run(a...);
         case K_FP16:
             if (ip) return lpr == 1 ? F<K_FP16, M_IP, 1>::run(a...) : F<K_FP16, M_IP, 4>::run(a...);
             return lpr == 1 ? F<K_FP16, M_L2, 1>::run(a...) : F<K_FP16, M_L2, 4>::run(a...);
