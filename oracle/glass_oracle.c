@@ -25,6 +25,8 @@ int go_layout(int kind, int d, int *dalign, int *csize) {
         case GO_SQ4U: align = 128; nbits = 4; break;  /* sq4u_quant.hpp:13  Quantizer<metric,128,4> */
         case GO_SQ2U: align = 256; nbits = 2; break;  /* sq2u_quant.hpp:11  Quantizer<metric,256,2> */
         case GO_SQ8: align = 16; nbits = 8; break;    /* sq8_quant.hpp:15-16 Quantizer<metric,16,8> */
+        case GO_SQ4UA: align = 128; nbits = 4; break; /* sq4ua_quant.hpp:13  Quantizer<metric,128,4> */
+        case GO_SQ1: align = 512; nbits = 1; break;   /* sq1_quant.hpp:16   Quantizer<metric,512,1> */
         case GO_E5M2: align = 16; nbits = 8; break;   /* e5m2_quant.hpp:11  Quantizer<metric,16,8> */
         case GO_FP16: align = 16; nbits = 16; break;  /* fp16_quant.hpp:10-16 (no AVX512-FP16 build macro) */
         case GO_BF16: align = 16; nbits = 16; break;  /* bf16_quant.hpp:9-15 (no AVX512-BF16 build macro) */
@@ -127,6 +129,12 @@ void go_train(int kind, int metric, const float *data, int64_t n, int d, float *
         } else {
             p[0] = find_absmax(data, nitems);     /* calibrator.hpp:511-514 */
         }
+    } else if (kind == GO_SQ4UA) {
+        /* sq4ua_quant.hpp:18,26: all n*d floats, drop 1% at each end */
+        float mn, mx;
+        find_minmax(data, n * (int64_t)d, 0.01f, &mn, &mx);
+        p[0] = mn;
+        p[1] = mx - mn;
     } else if (kind == GO_SQ4U || kind == GO_SQ2U) {
         /* sq4u_quant.hpp:307-309, sq2u_quant.hpp:27-29: nitems = (int64)(n*d*0.1f) - an int64*float
          * product - then drop 1% (SQ4U) or 5% (SQ2U) at each end */
@@ -236,7 +244,10 @@ static void encode_row(int kind, int metric, const float *p, const float *x, int
         } else {
             for (int j = 0; j < d; ++j) out[j] = (uint8_t)(int8_t)sym_code(x[j], p[0], 127);
         }
-    } else if (kind == GO_SQ4U) {                    /* sq4u_quant.hpp:319-329: even dim -> low nibble */
+    } else if (kind == GO_SQ1) {                     /* sq1_quant.hpp:36-42: bit j%8 of byte j/8 = (x > 0) */
+        for (int j = 0; j < d; ++j)
+            if (x[j] > 0) out[j / 8] |= (uint8_t)(1u << (j % 8));
+    } else if (kind == GO_SQ4U || kind == GO_SQ4UA) { /* sq4u_quant.hpp:319-329: even dim -> low nibble */
         for (int j = 0; j < d; ++j) {
             uint8_t y = (uint8_t)affine_code(x[j], p[0], p[1], 15);
             out[j / 2] |= (j & 1) ? (uint8_t)(y << 4) : y;
@@ -277,7 +288,12 @@ void go_encode(int kind, int metric, const float *p, const float *data, int64_t 
 int go_encode_query(int kind, int metric, const float *p, const float *q, int d, void *out) {
     int dalign, csize;
     go_layout(kind, d, &dalign, &csize);
-    if (kind == GO_SQ8U || kind == GO_SQ4U || kind == GO_SQ2U) {
+    if (kind == GO_SQ4UA) {                          /* sq4ua_quant.hpp:52-58 encode8: transform(x, 127), bytes */
+        memset(out, 0, (size_t)dalign);
+        for (int j = 0; j < d; ++j) ((uint8_t *)out)[j] = (uint8_t)affine_code(q[j], p[0], p[1], 127);
+        return dalign;
+    }
+    if (kind == GO_SQ8U || kind == GO_SQ4U || kind == GO_SQ2U || kind == GO_SQ1) {
         encode_row(kind, metric, p, q, d, csize, d, (uint8_t *)out);
         return csize;
     }
@@ -321,6 +337,22 @@ double go_distance(int kind, int metric, const void *qenc, const uint8_t *code, 
         }
         for (int i = 0; i < dalign; ++i) s += (int32_t)x[i] * (int32_t)y[i];   /* dot_s8_s8_ref */
         return (double)(-s);
+    }
+    if (kind == GO_SQ4UA) {                           /* L2SqrSQ8SQ4 (glass/simd/avx512.hpp:146-158): the 4-bit code
+                                                         * c read as 8c+4 on the query's 0..127 scale */
+        const uint8_t *x = (const uint8_t *)qenc, *y = code;
+        int32_t s = 0;
+        for (int i = 0; i < dalign; ++i) {
+            int32_t c = (y[i / 2] >> ((i & 1) * 4)) & 15, t = (int32_t)x[i] - (8 * c + 4);
+            s += t * t;
+        }
+        return (double)s;
+    }
+    if (kind == GO_SQ1) {                             /* SQ1Quantizer::distf (sq1_quant.hpp:43-62): Hamming */
+        const uint8_t *x = (const uint8_t *)qenc, *y = code;
+        int32_t s = 0;
+        for (int i = 0; i < dalign / 8; ++i) s += __builtin_popcount((unsigned)(x[i] ^ y[i]));
+        return (double)s;
     }
     if (kind == GO_SQ2U) {                            /* l2a_u2_u2 (x86/l2_impl.hpp:301-333): L2 on 2-bit codes, both metrics */
         const uint8_t *x = (const uint8_t *)qenc, *y = code;

@@ -20,7 +20,8 @@ extern "C" {
 #endif
 
 /* Quantizer kinds (names follow glass/quant/quant.hpp:25-43). */
-enum { GO_FP32 = 0, GO_FP16 = 1, GO_BF16 = 2, GO_E5M2 = 3, GO_SQ8U = 4, GO_SQ8 = 5, GO_SQ4U = 7, GO_SQ2U = 11 };
+enum { GO_FP32 = 0, GO_FP16 = 1, GO_BF16 = 2, GO_E5M2 = 3, GO_SQ8U = 4, GO_SQ8 = 5, GO_SQ4U = 7, GO_SQ4UA = 8,
+       GO_SQ2U = 11, GO_SQ1 = 12 };
 /* Metrics (glass/common.hpp:13-19). */
 enum { GO_L2 = 0, GO_IP = 1 };
 

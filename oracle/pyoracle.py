@@ -22,10 +22,10 @@ ORACLE_SO = os.path.join(HERE, "_build", "libglass_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libglass_ref.so")
 REFERENCE_DIR = os.environ.get("GLASS_REFERENCE_DIR", "/root/reference")
 
-KIND = {"FP32": 0, "FP16": 1, "BF16": 2, "E5M2": 3, "SQ8U": 4, "SQ8": 5, "SQ4U": 7, "SQ2U": 11}
+KIND = {"FP32": 0, "FP16": 1, "BF16": 2, "E5M2": 3, "SQ8U": 4, "SQ8": 5, "SQ4U": 7, "SQ4UA": 8, "SQ2U": 11, "SQ1": 12}
 METRIC = {"L2": 0, "IP": 1}
 # get_refine_factor (glass/searcher/graph_searcher.hpp:227-238) for the quantizers in scope
-REFINE_FACTOR = {"SQ8U": 1.5, "SQ8": 1.5, "SQ4U": 1.5, "SQ2U": 3.0, "E5M2": 1.0, "FP32": 1.0, "FP16": 1.0, "BF16": 1.0}
+REFINE_FACTOR = {"SQ8U": 1.5, "SQ8": 1.5, "SQ4U": 1.5, "SQ4UA": 1.5, "SQ2U": 3.0, "SQ1": 3.0, "E5M2": 1.0, "FP32": 1.0, "FP16": 1.0, "BF16": 1.0}
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -112,7 +112,8 @@ class Quant:
 
     def encode_queries(self, q: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.d)
-        width = self.csize if self.quant in ("SQ8U", "SQ4U", "SQ2U") else (12 if self.quant == "SQ8" else 4) * self.dalign
+        width = {"SQ8U": self.csize, "SQ4U": self.csize, "SQ2U": self.csize, "SQ1": self.csize, "SQ4UA": self.dalign,
+                 "SQ8": 12 * self.dalign}.get(self.quant, 4 * self.dalign)
         out = np.zeros((q.shape[0], width), np.uint8)
         for i in range(q.shape[0]):
             _oracle_lib().go_encode_query(self.kind, self.m, self.params, q[i], self.d, out[i].ctypes.data)
@@ -148,6 +149,8 @@ class Searcher:
 
     def __init__(self, graph: Graph, data: np.ndarray, metric: str, quantizer: str, refine_quant: str = ""):
         data = np.ascontiguousarray(data, dtype=np.float32)
+        if quantizer == "SQ1" and metric != "IP":
+            raise ValueError("SQ1 searchers exist for IP only (graph_searcher.hpp:362-369)")
         self.graph = graph
         self.q = Quant(quantizer, metric, data)
         self.ef = 32

@@ -42,6 +42,14 @@ int with_quant(const std::string &quant, const std::string &metric, int d, Fn &&
         if (l2) { glass::SQ8Quantizer<Metric::L2> q(d); return fn(q); }
         glass::SQ8Quantizer<Metric::IP> q(d); return fn(q);
     }
+    if (quant == "SQ4UA") {
+        if (l2) { glass::SQ4QuantizerUniformAsym<Metric::L2> q(d); return fn(q); }
+        glass::SQ4QuantizerUniformAsym<Metric::IP> q(d); return fn(q);
+    }
+    if (quant == "SQ1") {
+        if (l2) { glass::SQ1Quantizer<Metric::L2> q(d); return fn(q); }
+        glass::SQ1Quantizer<Metric::IP> q(d); return fn(q);
+    }
     if (quant == "SQ2U") {
         if (l2) { glass::SQ2QuantizerUniform<Metric::L2> q(d); return fn(q); }
         glass::SQ2QuantizerUniform<Metric::IP> q(d); return fn(q);

@@ -44,7 +44,7 @@ def main():
         out[f"params/{quant}/{metric}"] = params
         d, _ = R.query_distances(quant, metric, base, queries[: spec.NQ_DIST], ids)
         out[f"dist/{quant}/{metric}"] = d
-        if quant in ("SQ8U", "SQ4U", "SQ2U", "SQ8"):
+        if quant in ("SQ8U", "SQ4U", "SQ2U", "SQ8", "SQ4UA", "SQ1"):
             d, _ = R.query_distances("FP32", metric, base, queries[: spec.NQ_DIST], ids)
             out[f"dist/FP32/{metric}"] = d
     for case in spec.search_cases():

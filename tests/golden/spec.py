@@ -9,7 +9,8 @@ NQ_DIST, NQ_SEARCH = 16, 60
 GRAPHS = {"hnsw_d100": ("HNSW", 16, 40), "nsg_d100": ("NSG", 16, 40)}
 QUANTS = [("SQ8U", "L2"), ("SQ8U", "IP"), ("SQ4U", "L2"), ("SQ4U", "IP"), ("E5M2", "L2"), ("E5M2", "IP"),
           ("FP32", "L2"), ("FP32", "IP"), ("FP16", "L2"), ("FP16", "IP"), ("BF16", "L2"), ("BF16", "IP"),
-          ("SQ2U", "L2"), ("SQ2U", "IP"), ("SQ8", "L2"), ("SQ8", "IP")]
+          ("SQ2U", "L2"), ("SQ2U", "IP"), ("SQ8", "L2"), ("SQ8", "IP"), ("SQ4UA", "L2"), ("SQ4UA", "IP"),
+          ("SQ1", "L2"), ("SQ1", "IP")]
 # (quant, metric, refine)
 SEARCHERS = [("SQ8U", "L2", ""), ("SQ8U", "IP", ""), ("SQ4U", "L2", "FP32"), ("SQ4U", "IP", "FP32"),
              ("E5M2", "L2", ""), ("E5M2", "IP", ""), ("FP32", "L2", ""), ("FP32", "IP", ""), ("SQ8U", "L2", "FP32"),
@@ -17,7 +18,9 @@ SEARCHERS = [("SQ8U", "L2", ""), ("SQ8U", "IP", ""), ("SQ4U", "L2", "FP32"), ("S
              # make_refiner: an FP16 store; a known quantizer without a refiner; a name the map lacks (FP32)
              ("SQ4U", "L2", "FP16"), ("SQ8U", "IP", "FP16"), ("SQ4U", "L2", "BF16"), ("SQ4U", "IP", "FP64"),
              ("SQ2U", "L2", ""), ("SQ2U", "L2", "FP32"), ("SQ2U", "IP", "FP32"),
-             ("SQ8", "L2", ""), ("SQ8", "IP", ""), ("SQ8", "L2", "FP32")]
+             ("SQ8", "L2", ""), ("SQ8", "IP", ""), ("SQ8", "L2", "FP32"),
+             ("SQ4UA", "L2", ""), ("SQ4UA", "L2", "FP32"), ("SQ4UA", "IP", "FP32"), ("SQ1", "IP", ""),
+             ("SQ1", "IP", "FP32")]  # SQ1 searchers exist for IP only (graph_searcher.hpp:362-369)
 # (ef, k): includes k > ef, the case where search and batch_search differ (graph_searcher.hpp:134,152)
 EFK = [(16, 10), (40, 10), (8, 20)]
 

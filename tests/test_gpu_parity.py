@@ -41,7 +41,7 @@ def test_codes_and_calibration(gpu, golden, quant, metric):
 
 @pytest.mark.parametrize("quant,metric", spec.QUANTS)
 def test_distances_bit_exact(gpu, golden, quant, metric):
-    refine = "FP32" if quant in ("SQ8U", "SQ4U", "SQ2U", "SQ8") else ""
+    refine = "FP32" if quant in ("SQ8U", "SQ4U", "SQ2U", "SQ8", "SQ4UA", "SQ1") else ""
     s = searcher(gpu, "nsg_d100", quant, metric, refine)
     q = spec.queries()[: spec.NQ_DIST]
     d = s.distances(q, golden["dist_ids"])
