@@ -66,9 +66,9 @@ void gsx_graph_destroy(gsx_graph *g);
 /* ---- searchers: GraphSearcherBase (glass/searcher/searcher_base.hpp:7-19) ---------------- */
 
 /* create_searcher(graph, metric, quantizer, refine_quant) (graph_searcher.hpp:256-391).
- * metric "L2" | "IP"; quantizer "SQ8U" | "SQ8" | "SQ4U" | "SQ2U" | "E5M2" | "FP32" | "FP16" |
- * "BF16" (an unknown name selects FP32, as the reference's quantizer_map does; SQ6, SQ4, SQ4UA, SQ8P,
- * SQ1 and PQ8 return GSX_ERR_UNSUPPORTED); refine_quant as make_refiner reads it
+ * metric "L2" | "IP"; quantizer "SQ8U" | "SQ8" | "SQ4U" | "SQ4UA" | "SQ2U" | "SQ1" (IP only, as
+ * in the reference) | "E5M2" | "FP32" | "FP16" | "BF16" (an unknown name selects FP32, as the
+ * reference's quantizer_map does; SQ6, SQ4, SQ8P and PQ8 return GSX_ERR_UNSUPPORTED); refine_quant as make_refiner reads it
  * (graph_searcher.hpp:227-254): "" none, "FP16" an FP16 store, "FP32" or a name the quantizer map
  * lacks an FP32 store, any other known name no refiner; "SQ8U" / "SQ8" with an SQ quantizer return
  * GSX_ERR_UNSUPPORTED.  The graph's contents move into the searcher (python/bindings.cc:98); *graph

@@ -103,6 +103,8 @@ cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, in
     uint32_t *o = reinterpret_cast<uint32_t *>(out);
     if (kind == K_SQ4U) encode_rows<K_SQ4U, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
     else if (kind == K_SQ2U) encode_rows<K_SQ2U, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
+    else if (kind == K_SQ4UA) encode_rows<K_SQ4UA, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
+    else if (kind == K_SQ1) encode_rows<K_SQ1, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
     else if (kind == K_SQ8U && metric == M_IP) encode_rows<K_SQ8U, M_IP><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
     else if (kind == K_SQ8U) encode_rows<K_SQ8U, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);
     else if (kind == K_E5M2) encode_rows<K_E5M2, M_L2><<<g, 256, 0, st>>>(data, n, d, csize, p0, p1, o);

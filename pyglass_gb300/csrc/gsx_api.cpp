@@ -73,11 +73,13 @@ namespace {
 
 // quantizer_map (glass/quant/quant.hpp:25-43); operator[] on an unknown key yields FP32.
 int parse_quant(const std::string &q, int *kind) {
-    static const char *unsupported[] = {"SQ6", "SQ4UA", "SQ4", "SQ8P", "SQ1", "PQ8"};
+    static const char *unsupported[] = {"SQ6", "SQ4", "SQ8P", "PQ8"};
     if (q == "SQ8U") *kind = K_SQ8U;
     else if (q == "SQ4U") *kind = K_SQ4U;
     else if (q == "SQ2U") *kind = K_SQ2U;
     else if (q == "SQ8") *kind = K_SQ8;
+    else if (q == "SQ4UA") *kind = K_SQ4UA;
+    else if (q == "SQ1") *kind = K_SQ1;
     else if (q == "E5M2") *kind = K_E5M2;
     else if (q == "FP16") *kind = K_FP16;
     else if (q == "BF16") *kind = K_BF16;
@@ -95,6 +97,8 @@ int layout(int kind, int d, int *dalign, int *csize) {
     else if (kind == K_SQ4U) { align = 128; nbits = 4; }
     else if (kind == K_SQ2U) { align = 256; nbits = 2; }  // sq2u_quant.hpp:11
     else if (kind == K_SQ8) { align = 16; nbits = 8; }    // sq8_quant.hpp:15-16
+    else if (kind == K_SQ4UA) { align = 128; nbits = 4; } // sq4ua_quant.hpp:13
+    else if (kind == K_SQ1) { align = 512; nbits = 1; }   // sq1_quant.hpp:16
     else if (kind == K_E5M2) { align = 16; nbits = 8; }
     // fp16_quant.hpp:10-16, bf16_quant.hpp:9-15: align 16 unless built with AVX512-FP16/BF16 macros that
     // the reference's build never defines
@@ -133,7 +137,7 @@ int device_kth2(const float *x, int64_t n, int64_t r0, int64_t r1, unsigned *scr
 // smallest and top-th largest.
 int calibrate(int kind, int metric, const float *x, int64_t n, int d, float *p, DevBuf &scratch, cudaStream_t st) {
     p[0] = p[1] = 0.0f;
-    if (kind != K_SQ8U && kind != K_SQ4U && kind != K_SQ2U) return GSX_OK;
+    if (kind != K_SQ8U && kind != K_SQ4U && kind != K_SQ2U && kind != K_SQ4UA) return GSX_OK;
     int rc = scratch.ensure(512 * sizeof(unsigned));
     if (rc) return rc;
     unsigned *w = scratch.as<unsigned>();
@@ -152,10 +156,11 @@ int calibrate(int kind, int metric, const float *x, int64_t n, int d, float *p, 
         }
         return GSX_OK;
     }
-    int64_t nitems = (int64_t)((float)(n * (int64_t)d) * 0.1f);
+    // SQ4U / SQ2U train on the first 10%, SQ4UA on all n*d floats (sq4ua_quant.hpp:26)
+    int64_t nitems = kind == K_SQ4UA ? n * (int64_t)d : (int64_t)((float)(n * (int64_t)d) * 0.1f);
     if (nitems < 1) nitems = 1;
     // find_minmax's drop ratio: 1% for SQ4U, 5% for SQ2U (sq2u_quant.hpp:16-29)
-    int64_t top = (int64_t)((float)nitems * (kind == K_SQ2U ? 0.05f : 0.01f)) + 1;
+    int64_t top = (int64_t)((float)nitems * (kind == K_SQ2U ? 0.05f : 0.01f)) + 1;  // SQ4UA: 1% as well
     if (top > nitems) top = nitems;
     float mn = 0.0f, mx = 0.0f;
     if ((rc = device_kth2(x, nitems, top - 1, nitems - top, w, st, &mn, &mx))) return rc;
@@ -590,7 +595,9 @@ int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quanti
     const std::string rq = refine_quant ? refine_quant : "";
     // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ8/SQ4U, 3 for SQ2U, 1.0 otherwise (in which
     // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
-    const float factor = kind == K_SQ2U ? 3.0f : (kind == K_SQ8U || kind == K_SQ4U || kind == K_SQ8) ? 1.5f : 1.0f;
+    const float factor = (kind == K_SQ2U || kind == K_SQ1)                                           ? 3.0f
+                         : (kind == K_SQ8U || kind == K_SQ4U || kind == K_SQ8 || kind == K_SQ4UA) ? 1.5f
+                                                                                                  : 1.0f;
     // make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer map
     // does not know -> FP32 store; SQ8U / SQ8 -> their own refiners; any other known name -> none
     int rkind = K_FP32;
@@ -605,6 +612,8 @@ int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quanti
             return fail(GSX_ERR_UNSUPPORTED, "refine quantizer %s is outside the GPU search path", rq.c_str());
         if (rq == "SQ8U" || rq == "SQ8") refiner = false;  // factor 1: the refiner only forwards
     }
+    if (kind == K_SQ1 && !(metric && std::string(metric) == "IP"))  // graph_searcher.hpp:362-369
+        return fail(GSX_ERR_UNSUPPORTED, "SQ1 searchers exist for the IP metric only");
     auto *s = new gsx_searcher;
     s->kind = kind;
     // metric_map (common.hpp:13-19): unknown names fall on the default-constructed L2

@@ -29,7 +29,8 @@ __device__ __forceinline__ float dist_of_key_float(uint32_t k) {
 
 template <int KIND>
 struct IsIntKind {
-    static constexpr bool value = (KIND == K_SQ8U || KIND == K_SQ4U || KIND == K_SQ2U);
+    static constexpr bool value =
+        (KIND == K_SQ8U || KIND == K_SQ4U || KIND == K_SQ2U || KIND == K_SQ4UA || KIND == K_SQ1);
 };
 
 // ---- query encoding ---------------------------------------------------------------------------
@@ -62,7 +63,15 @@ __device__ __forceinline__ uint32_t sq_code_byte(const float *x, int d, int b, f
             if (j < d) byte |= (uint32_t)affine_code(x[j], p0, p1, 3.0f) << (2 * k);
         }
         return byte;
-    } else if (KIND == K_SQ4U) {  // sq4u_quant.hpp:319-329: even dim -> low nibble
+    } else if (KIND == K_SQ1) {  // sq1_quant.hpp:36-42: bit j%8 of byte j/8 = (x > 0)
+        uint32_t byte = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int j = 8 * b + k;
+            if (j < d && x[j] > 0.0f) byte |= 1u << k;
+        }
+        return byte;
+    } else if (KIND == K_SQ4U || KIND == K_SQ4UA) {  // sq4u_quant.hpp:319-329: even dim -> low nibble
         int j0 = 2 * b, j1 = 2 * b + 1;
         uint32_t lo = j0 < d ? (uint32_t)affine_code(x[j0], p0, p1, 15.0f) : 0u;
         uint32_t hi = j1 < d ? (uint32_t)affine_code(x[j1], p0, p1, 15.0f) : 0u;
@@ -99,6 +108,9 @@ __device__ __forceinline__ int32_t team_sum(int32_t v) {
 //   SQ4U: words [0, nw) = low nibbles of the query code (0x0F0F0F0F lanes), [nw, 2nw) = high
 //         nibbles; nw = csize/4.  Sum of squares of all nibbles in qsq.
 //   SQ8U: words [0, nw) = the code bytes.  L2 also uses qsq.
+//   SQ4UA: the query is coded on 0..127 (transform(x, 127)); words [0, nw) hold its even dimensions
+//         and [nw, 2nw) its odd ones, in the byte order of the base words' low / high nibbles.
+//   SQ1:  words [0, nw) = the query's sign bits.
 //   SQ2U: words [k*nw, (k+1)*nw), k = 0..3 = the query's 2-bit codes at bits 2k of each byte, one per
 //         byte (0x03030303 lanes); qsq as for SQ4U.
 // SQ2U word: the four 2-bit planes against the query's planes (l2a_u2_u2, helpa x86/l2_impl.hpp:301-333).
@@ -109,6 +121,15 @@ __device__ __forceinline__ void sq2_word(uint32_t w, const uint32_t *qp, int nw,
         aa = __dp4a(x, x, aa);
         ab = __dp4a(x, qp[k * nw], ab);
     }
+}
+
+// SQ4UA word (L2SqrSQ8SQ4, glass/simd/avx512.hpp:146-158): code c read as 8c+4 on the 0..127 scale.
+__device__ __forceinline__ void sq4a_word(uint32_t w, uint32_t qe, uint32_t qo, uint32_t &aa, uint32_t &ab) {
+    const uint32_t ylo = ((w & 0x0F0F0F0Fu) << 3) + 0x04040404u, yhi = (((w >> 4) & 0x0F0F0F0Fu) << 3) + 0x04040404u;
+    aa = __dp4a(ylo, ylo, aa);
+    aa = __dp4a(yhi, yhi, aa);
+    ab = __dp4a(ylo, qe, ab);
+    ab = __dp4a(yhi, qo, ab);
 }
 
 __device__ __forceinline__ void sq4_word(uint32_t w, uint32_t ql, uint32_t qh, uint32_t &aa, uint32_t &ab) {
@@ -124,7 +145,29 @@ __device__ __forceinline__ int32_t sq_partial(const uint8_t *__restrict__ codes,
                                              const uint32_t *qc) {
     const uint4 *row = reinterpret_cast<const uint4 *>(codes + (size_t)id * (size_t)csize);
     const int nch = csize >> 4;
-    if (KIND == K_SQ2U) {
+    if (KIND == K_SQ4UA) {
+        const uint4 *qe = reinterpret_cast<const uint4 *>(qc);
+        const uint4 *qo = reinterpret_cast<const uint4 *>(qc + (csize >> 2));
+        uint32_t aa = 0, ab = 0;
+#pragma unroll 4
+        for (int c = sub; c < nch; c += LPR) {
+            const uint4 v = __ldg(row + c);
+            const uint4 e = qe[c], o = qo[c];
+            sq4a_word(v.x, e.x, o.x, aa, ab);
+            sq4a_word(v.y, e.y, o.y, aa, ab);
+            sq4a_word(v.z, e.z, o.z, aa, ab);
+            sq4a_word(v.w, e.w, o.w, aa, ab);
+        }
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (KIND == K_SQ1) {
+        const uint4 *qv = reinterpret_cast<const uint4 *>(qc);
+        int32_t s = 0;
+        for (int c = sub; c < nch; c += LPR) {
+            const uint4 v = __ldg(row + c), q = qv[c];
+            s += __popc(v.x ^ q.x) + __popc(v.y ^ q.y) + __popc(v.z ^ q.z) + __popc(v.w ^ q.w);
+        }
+        return s;
+    } else if (KIND == K_SQ2U) {
         const int nw = csize >> 2;
         uint32_t aa = 0, ab = 0;
 #pragma unroll 2
@@ -184,7 +227,29 @@ __device__ __forceinline__ int32_t sq_partial(const uint8_t *__restrict__ codes,
 // arithmetic as sq_partial with one lane.
 template <int KIND, int METRIC>
 __device__ __forceinline__ int32_t sq_partial_row(const uint4 *row, int nch, const uint32_t *qc) {
-    if (KIND == K_SQ2U) {
+    if (KIND == K_SQ4UA) {
+        const uint4 *qe = reinterpret_cast<const uint4 *>(qc);
+        const uint4 *qo = reinterpret_cast<const uint4 *>(qc + 4 * nch);
+        uint32_t aa = 0, ab = 0;
+#pragma unroll 4
+        for (int c = 0; c < nch; ++c) {
+            const uint4 v = row[c];
+            const uint4 e = qe[c], o = qo[c];
+            sq4a_word(v.x, e.x, o.x, aa, ab);
+            sq4a_word(v.y, e.y, o.y, aa, ab);
+            sq4a_word(v.z, e.z, o.z, aa, ab);
+            sq4a_word(v.w, e.w, o.w, aa, ab);
+        }
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (KIND == K_SQ1) {
+        const uint4 *qv = reinterpret_cast<const uint4 *>(qc);
+        int32_t s = 0;
+        for (int c = 0; c < nch; ++c) {
+            const uint4 v = row[c], q = qv[c];
+            s += __popc(v.x ^ q.x) + __popc(v.y ^ q.y) + __popc(v.z ^ q.z) + __popc(v.w ^ q.w);
+        }
+        return s;
+    } else if (KIND == K_SQ2U) {
         const int nw = 4 * nch;
         uint32_t aa = 0, ab = 0;
 #pragma unroll 2
@@ -245,6 +310,7 @@ template <int KIND, int METRIC, int LPR>
 __device__ __forceinline__ int32_t sq_finish(int32_t partial, int32_t qsq) {
     int32_t s = team_sum<LPR>(partial);
     if (KIND == K_SQ8U && METRIC == M_IP) return -s;
+    if (KIND == K_SQ1) return s;  // Hamming distance, no query term
     return qsq + s;
 }
 

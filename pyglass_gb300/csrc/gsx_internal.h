@@ -8,7 +8,9 @@
 namespace gsx {
 
 // Quantizer kinds and metrics (values follow glass/quant/quant.hpp:25-43 and glass/common.hpp).
-enum Kind : int { K_FP32 = 0, K_FP16 = 1, K_BF16 = 2, K_E5M2 = 3, K_SQ8U = 4, K_SQ8 = 5, K_SQ4U = 7, K_SQ2U = 11 };
+enum Kind : int {
+    K_FP32 = 0, K_FP16 = 1, K_BF16 = 2, K_E5M2 = 3, K_SQ8U = 4, K_SQ8 = 5, K_SQ4U = 7, K_SQ4UA = 8, K_SQ2U = 11, K_SQ1 = 12
+};
 
 // Kinds whose codes decode to floats compared against the fp32 query (the float engines).
 // SQ8 (per-dimension affine codes) decodes each code to a float with its dimension's min and dif.

@@ -479,6 +479,24 @@ __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState 
     const int nw = ix.csize >> 2;
     int32_t sq = 0;
     for (int wi = lane; wi < nw; wi += 32) {
+        if (KIND == K_SQ4UA) {
+            // sq4ua_quant.hpp:52-58 (encode8): each dimension on 0..127; base word wi holds dimensions
+            // 8wi..8wi+7, the even ones in its low nibbles and the odd ones in its high nibbles
+            uint32_t qe = 0, qo = 0;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int j0 = 8 * wi + 2 * t, j1 = j0 + 1;
+                const uint32_t c0 = j0 < ix.d ? (uint32_t)affine_code(w.fq[j0], ix.p0, ix.p1, 127.0f) : 0u;
+                const uint32_t c1 = j1 < ix.d ? (uint32_t)affine_code(w.fq[j1], ix.p0, ix.p1, 127.0f) : 0u;
+                qe |= c0 << (8 * t);
+                qo |= c1 << (8 * t);
+            }
+            w.qc[wi] = qe;
+            w.qc[nw + wi] = qo;
+            sq = __dp4a(qe, qe, (uint32_t)sq);
+            sq = __dp4a(qo, qo, (uint32_t)sq);
+            continue;
+        }
         uint32_t word = 0;
 #pragma unroll
         for (int t = 0; t < 4; ++t)
@@ -920,6 +938,14 @@ template <template <int, int, int> class F, typename... A>
 auto dispatch(int kind, int metric, int lpr, A &&...a) {
     const bool ip = metric == M_IP;
     switch (kind) {
+        case K_SQ4UA:  // L2SqrSQ8SQ4 for both metrics (sq4ua_quant.hpp:48)
+            if (lpr >= 4) return F<K_SQ4UA, M_L2, 4>::run(a...);
+            if (lpr == 2) return F<K_SQ4UA, M_L2, 2>::run(a...);
+            return F<K_SQ4UA, M_L2, 1>::run(a...);
+        case K_SQ1:  // Hamming for both metrics (sq1_quant.hpp:64)
+            if (lpr >= 4) return F<K_SQ1, M_L2, 4>::run(a...);
+            if (lpr == 2) return F<K_SQ1, M_L2, 2>::run(a...);
+            return F<K_SQ1, M_L2, 1>::run(a...);
         case K_SQ2U:  // L2 on codes for both metrics (sq2u_quant.hpp:55)
             if (lpr >= 4) return F<K_SQ2U, M_L2, 4>::run(a...);
             if (lpr == 2) return F<K_SQ2U, M_L2, 2>::run(a...);
@@ -1000,7 +1026,7 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     L->fq = off; off += fq * 4;
     L->fq_len = fq;
     L->qc = off;
-    if (ix.kind == K_SQ4U) off += up(2 * ix.csize, 16);
+    if (ix.kind == K_SQ4U || ix.kind == K_SQ4UA) off += up(2 * ix.csize, 16);
     else if (ix.kind == K_SQ2U) off += up(4 * ix.csize, 16);
     else if (ix.kind == K_SQ8U) off += up(ix.csize, 16);
     L->table = off;
@@ -1008,7 +1034,8 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     off = up(off, 16);
     L->stage = off;
     L->stage_row = 0;
-    if ((ix.kind == K_SQ4U || ix.kind == K_SQ8U || ix.kind == K_SQ2U) && !(prefetch & kNoStageCodes) && ix.csize <= 128 &&
+    if ((ix.kind == K_SQ4U || ix.kind == K_SQ8U || ix.kind == K_SQ2U || ix.kind == K_SQ4UA || ix.kind == K_SQ1) &&
+        !(prefetch & kNoStageCodes) && ix.csize <= 128 &&
         ix.csize % 16 == 0) {
         L->stage_row = ix.csize;
         off += 32 * ix.csize;

@@ -32,7 +32,7 @@ def tiny_graph():
 
 
 @pytest.mark.parametrize("name", ["normal37", "ties128", "tiny", "outliers96"])
-@pytest.mark.parametrize("quant,metric", [("SQ8U", "L2"), ("SQ8U", "IP"), ("SQ4U", "L2"), ("SQ4U", "IP"), ("SQ2U", "L2")])
+@pytest.mark.parametrize("quant,metric", [("SQ8U", "L2"), ("SQ8U", "IP"), ("SQ4U", "L2"), ("SQ4U", "IP"), ("SQ2U", "L2"), ("SQ4UA", "L2")])
 def test_device_calibration_matches_oracle(gpu, oracle, tiny_graph, name, quant, metric):
     x = datasets()[name]
     s = gpu.Searcher(gpu.Graph(tiny_graph), x, metric, quant)
