@@ -13,6 +13,19 @@ enum Kind : int {
 };
 
 // Kinds whose codes decode to floats compared against the fp32 query (the float engines).
+// Bytes of shared memory the encoded query of an integer kind takes (prepare_query's layout): two
+// planes for the 4-bit kinds, four for SQ2U, the code itself for SQ8U and SQ1; 0 for float kinds.
+inline int query_code_bytes(int kind, int csize) {
+    switch (kind) {
+        case K_SQ4U:
+        case K_SQ4UA: return 2 * csize;
+        case K_SQ2U: return 4 * csize;
+        case K_SQ8U:
+        case K_SQ1: return csize;
+        default: return 0;
+    }
+}
+
 // SQ8 (per-dimension affine codes) decodes each code to a float with its dimension's min and dif.
 inline bool is_float_kind(int k) { return k == K_FP32 || k == K_FP16 || k == K_BF16 || k == K_E5M2 || k == K_SQ8; }
 enum MetricId : int { M_L2 = 0, M_IP = 1 };

@@ -1026,9 +1026,7 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     L->fq = off; off += fq * 4;
     L->fq_len = fq;
     L->qc = off;
-    if (ix.kind == K_SQ4U || ix.kind == K_SQ4UA) off += up(2 * ix.csize, 16);
-    else if (ix.kind == K_SQ2U) off += up(4 * ix.csize, 16);
-    else if (ix.kind == K_SQ8U) off += up(ix.csize, 16);
+    off += up(query_code_bytes(ix.kind, ix.csize), 16);
     L->table = off;
     if (table_bits > 0) off += (1 << table_bits) * 4;
     off = up(off, 16);

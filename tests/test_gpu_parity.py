@@ -30,7 +30,7 @@ def searcher(gpu, g, quant, metric, refine=""):
     return _cache[key]
 
 
-@pytest.mark.parametrize("quant,metric", spec.QUANTS)
+@pytest.mark.parametrize("quant,metric", spec.SEARCHABLE)
 def test_codes_and_calibration(gpu, golden, quant, metric):
     s = searcher(gpu, "nsg_d100", quant, metric)
     cs, params = s.calibration()
@@ -39,7 +39,7 @@ def test_codes_and_calibration(gpu, golden, quant, metric):
     np.testing.assert_array_equal(np.array(params, np.float32), golden[f"params/{quant}/{metric}"])
 
 
-@pytest.mark.parametrize("quant,metric", spec.QUANTS)
+@pytest.mark.parametrize("quant,metric", spec.SEARCHABLE)
 def test_distances_bit_exact(gpu, golden, quant, metric):
     refine = "FP32" if quant in ("SQ8U", "SQ4U", "SQ2U", "SQ8", "SQ4UA", "SQ1") else ""
     s = searcher(gpu, "nsg_d100", quant, metric, refine)
@@ -246,3 +246,10 @@ def test_plain_c_abi(gpu):
     ref = searcher(gpu, "nsg_d100", "SQ4U", "L2", "FP32")
     ref.set_ef(16)
     np.testing.assert_array_equal(ids, ref.batch_search(q, 10)[0])
+
+
+def test_sq1_searcher_needs_ip(gpu):
+    """The reference builds SQ1 searchers for the IP metric only (graph_searcher.hpp:362-369)."""
+    graph = gpu.Graph(os.path.join(GOLDEN_DIR, "nsg_d100.glass"))
+    with pytest.raises(RuntimeError, match="IP metric only"):
+        gpu.Searcher(graph, spec.base(), "L2", "SQ1")
