@@ -14,7 +14,9 @@
 //   warp 1      TMEM allocation (256 columns = two 128x128 fp32 accumulators) and the MMA issuer
 //               (one elected thread, tcgen05.mma kind::f16, M=128 N=128 K=16)
 //   warps 4-11  epilogue: tcgen05.ld of the accumulator (warp w reads TMEM lanes 32*(w%4).., half
-//               (w-4)/4 of the columns), distance, per-query candidate list in shared memory
+//               (w-4)/4 of the columns), distance = fma(neg_scale, score, bias) for 32 columns at a
+//               time, and only when their minimum beats the list's threshold the per-query candidate
+//               list in shared memory
 // Every mbarrier wait is bounded; on timeout the CTA records an error and leaves after its copies
 // have drained, freeing its TMEM.
 #include <cuda.h>
@@ -42,7 +44,8 @@ struct KnnParams {
     int n_mt, n_chunks, tiles_per_chunk, n_tiles;
     int passes;                   // 1 (exact bf16 inputs) or 3 (hi/lo split)
     int ip;                       // 1 = inner product
-    const float *xnorm;           // N, |x|^2 (L2)
+    float neg_scale;              // -2 (L2) or -1 (IP): approximate distance = bias + neg_scale * score
+    const float *bias;            // n_tiles*kTN: |x|^2 (L2) or 0 (IP) per base row, +inf past N
     int32_t *cand;                // nq x n_chunks x 2 x kCand ids (-1 = none)
     float *cand_d;                // matching approximate distances
     unsigned *error;              // set on a timed-out wait
@@ -256,15 +259,33 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                 if (!mbar_wait(&tfull[ab], (it >> 1) & 1)) { ok = false; break; }
                 fence_after();
                 for (int c = 0; c < kTN / 64; ++c) {
+                    const int n0 = t * kTN + half * (kTN / 2) + c * 32;
+                    // the 32 columns' bias: the same addresses in every lane (broadcast loads), issued
+                    // before the accumulator read
+                    float b[32];
+                    const float4 *b4 = reinterpret_cast<const float4 *>(P.bias + n0);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const float4 x = __ldg(b4 + i);
+                        b[4 * i] = x.x;
+                        b[4 * i + 1] = x.y;
+                        b[4 * i + 2] = x.z;
+                        b[4 * i + 3] = x.w;
+                    }
                     float v[32];
                     const uint32_t col0 = (uint32_t)(ab * kTN + half * (kTN / 2) + c * 32);
                     tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + col0, v);
-                    const int n0 = t * kTN + half * (kTN / 2) + c * 32;
+                    float dmin = __int_as_float(0x7f800000);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        v[j] = fmaf(P.neg_scale, v[j], b[j]);
+                        dmin = fminf(dmin, v[j]);
+                    }
+                    if (!(dmin < thr)) continue;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const int n = n0 + j;
-                        const float dist = n >= P.N ? __int_as_float(0x7f800000)
-                                           : (P.ip ? -v[j] : __ldg(P.xnorm + n) - 2.0f * v[j]);
+                        const float dist = v[j];
                         if (dist < thr) {
                             // insert into the ascending list, dropping its last entry
                             int pos = kCand - 1;
@@ -317,6 +338,12 @@ __global__ void split_bf16(const float *__restrict__ x, int64_t n, int d, int dp
         cnt += rest != 0.0f;
     }
     if (cnt) atomicAdd(inexact, cnt);
+}
+
+// bias[n] = |x_n|^2 (L2) or 0 (IP) for n < N, +inf for the padding up to total
+__global__ void make_bias(const float *__restrict__ xn, int64_t N, int ip, int64_t total, float *__restrict__ bias) {
+    for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < total; n += (int64_t)gridDim.x * blockDim.x)
+        bias[n] = n < N ? (ip ? 0.0f : xn[n]) : __int_as_float(0x7f800000);
 }
 
 __global__ void row_norms(const float *__restrict__ x, int64_t n, int d, float *__restrict__ out) {
@@ -410,7 +437,7 @@ extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const fl
     if (N > (int64_t)INT32_MAX) return fail(GSX_ERR_INVALID, "N too large");
     cudaStream_t st = (cudaStream_t)stream;
     const int dp = 128;  // two 64-element K blocks
-    DevBuf xh, xl, qh, ql, xn, cand, cand_d, cnt;
+    DevBuf xh, xl, qh, ql, xn, bias, cand, cand_d, cnt;
     int rc;
     if ((rc = xh.ensure((size_t)N * dp * 2)) || (rc = xl.ensure((size_t)N * dp * 2)) ||
         (rc = qh.ensure((size_t)nq * dp * 2)) || (rc = ql.ensure((size_t)nq * dp * 2)) || (rc = xn.ensure((size_t)N * 4)) ||
@@ -442,7 +469,12 @@ extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const fl
     P.n_chunks = (P.n_tiles + P.tiles_per_chunk - 1) / P.tiles_per_chunk;
     P.passes = inexact ? 3 : 1;
     P.ip = ip ? 1 : 0;
-    P.xnorm = xn.as<float>();
+    P.neg_scale = ip ? -1.0f : -2.0f;
+    const int64_t nbias = (int64_t)P.n_tiles * kTN;
+    if ((rc = bias.ensure((size_t)nbias * 4))) return rc;
+    make_bias<<<1024, 256, 0, st>>>(xn.as<float>(), N, P.ip, nbias, bias.as<float>());
+    GSX_CUDA(cudaGetLastError());
+    P.bias = bias.as<float>();
     const size_t ncand = (size_t)P.n_chunks * 2 * kCand;
     if ((rc = cand.ensure((size_t)nq * ncand * 4)) || (rc = cand_d.ensure((size_t)nq * ncand * 4))) return rc;
     P.cand = cand.as<int32_t>();
