@@ -140,6 +140,21 @@ constexpr size_t kOpBytes = sizeof(KnnSmem);
 constexpr size_t kCandBytes = (size_t)kCand * kEpiWarps * 32 * 8;
 constexpr size_t kSmemBytes = kOpBytes + kCandBytes + 256 + 1024;
 
+// Inserts (dist, n) into this thread's ascending candidate list (stride kEpiWarps*32 in shared
+// memory), dropping the last entry; returns the new threshold (the last entry).  Kept out of line:
+// its 32 call sites in the unrolled epilogue would otherwise swamp the instruction cache.
+__device__ __noinline__ float cand_insert(float *cd, int32_t *ci, int slot, float dist, int n) {
+    int pos = kCand - 1;
+    while (pos > 0 && cd[(pos - 1) * kEpiWarps * 32 + slot] > dist) {
+        cd[pos * kEpiWarps * 32 + slot] = cd[(pos - 1) * kEpiWarps * 32 + slot];
+        ci[pos * kEpiWarps * 32 + slot] = ci[(pos - 1) * kEpiWarps * 32 + slot];
+        --pos;
+    }
+    cd[pos * kEpiWarps * 32 + slot] = dist;
+    ci[pos * kEpiWarps * 32 + slot] = n;
+    return cd[(kCand - 1) * kEpiWarps * 32 + slot];
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
 knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__ CUtensorMap tq_lo,
               const __grid_constant__ CUtensorMap tx_hi, const __grid_constant__ CUtensorMap tx_lo, KnnParams P) {
@@ -286,18 +301,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                     for (int j = 0; j < 32; ++j) {
                         const int n = n0 + j;
                         const float dist = v[j];
-                        if (dist < thr) {
-                            // insert into the ascending list, dropping its last entry
-                            int pos = kCand - 1;
-                            while (pos > 0 && cd[(pos - 1) * kEpiWarps * 32 + slot] > dist) {
-                                cd[pos * kEpiWarps * 32 + slot] = cd[(pos - 1) * kEpiWarps * 32 + slot];
-                                ci[pos * kEpiWarps * 32 + slot] = ci[(pos - 1) * kEpiWarps * 32 + slot];
-                                --pos;
-                            }
-                            cd[pos * kEpiWarps * 32 + slot] = dist;
-                            ci[pos * kEpiWarps * 32 + slot] = n;
-                            thr = cd[(kCand - 1) * kEpiWarps * 32 + slot];
-                        }
+                        if (dist < thr) thr = cand_insert(cd, ci, slot, dist, n);
                     }
                 }
                 fence_before();
