@@ -171,7 +171,12 @@ int ref_query_distances(const char *quant, const char *metric, const float *data
             if (qcodes) {
                 using X = typename std::decay_t<decltype(comp)>::X;
                 int nbytes = (int)(q.dim_align() * sizeof(X));
-                if constexpr (sizeof(X) == 1) nbytes = q.code_size();
+                // 1-byte query codes are code_size() bytes, except SQ4UA's, which are one byte per
+                // dimension (sq4ua_quant.hpp:52-58)
+                using Q = std::decay_t<decltype(q)>;
+                constexpr bool asym = std::is_same_v<Q, glass::SQ4QuantizerUniformAsym<glass::Metric::L2>> ||
+                                      std::is_same_v<Q, glass::SQ4QuantizerUniformAsym<glass::Metric::IP>>;
+                if constexpr (sizeof(X) == 1 && !asym) nbytes = q.code_size();
                 std::memcpy(qcodes + (int64_t)qi * qcode_stride, comp.q, std::min(nbytes, qcode_stride));
             }
         }
