@@ -63,3 +63,17 @@ def test_batch_order_changes_no_result(gpu, workload):
     np.testing.assert_array_equal(a_dis, b_dis)
     assert a_cmps == b_cmps
     np.testing.assert_array_equal(a_ids[: q.shape[0]], a_ids[q.shape[0]:][::-1])
+
+
+def test_clusters1m_fp16_matches_oracle(gpu, oracle, workload):
+    """FP16, the reference's default quantizer, at full size (1M rows of 256-byte codes)."""
+    base, q = workload
+    s = gpu.Searcher(gpu.Graph(*FOUND), base, "L2", "FP16")
+    o = oracle.Searcher(oracle_graph(oracle, gpu, *FOUND), base, "L2", "FP16")
+    s.set_ef(32)
+    o.set_ef(32)
+    gi, gd = s.batch_search(q, 10)
+    sample = np.arange(0, q.shape[0], 40)
+    oi, od = o.batch_search(q[sample], 10)
+    np.testing.assert_array_equal(gi[sample], oi)
+    np.testing.assert_array_equal(gd[sample], od)

@@ -76,7 +76,9 @@ def test_search_matches_reference(gpu, golden, case):
 
 @pytest.mark.parametrize("K", [5, 32, 48])
 @pytest.mark.parametrize("quant,metric,refine", [("SQ4U", "L2", "FP32"), ("SQ8U", "IP", ""), ("E5M2", "L2", ""),
-                                                 ("FP32", "IP", "")])
+                                                 ("FP32", "IP", ""), ("FP16", "L2", ""), ("BF16", "IP", ""),
+                                                 ("SQ2U", "L2", "FP32"), ("SQ4UA", "IP", "FP32"), ("SQ1", "IP", "FP32"),
+                                                 ("SQ8", "IP", "FP16"), ("SQ8", "L2", "")])
 def test_edge_graphs_match_oracle(gpu, oracle, tmp_path, K, quant, metric, refine):
     """Rows cut short by -1, repeated ids inside rows, several entry points with a repeat."""
     rng = np.random.default_rng(K)
