@@ -326,7 +326,15 @@ __device__ __forceinline__ int32_t sq_finish(int32_t partial, int32_t qsq) {
 // helpa reduction as FP32) widen exactly to fp32 before the arithmetic.
 // SQ8 (L2SqrSQ8_ext / IPSQ8_ext, glass/simd/avx512.hpp:40-75): y = fma(code + 0.5, dif, 256 min)
 // against 256 q (L2: (256q - y)^2, IP: q*y), glass's reduction; `ext` = mins[16*nsteps] then difs.
-template <int KIND, int METRIC, int LPR>
+// Row loads of the float engines: read-only global loads, or plain loads of a row staged in
+// shared memory (SMEM).
+template <bool SMEM, typename T>
+__device__ __forceinline__ T ld_row(const T *p) {
+    if constexpr (SMEM) return *p;
+    else return __ldg(p);
+}
+
+template <int KIND, int METRIC, int LPR, bool SMEM = false>
 __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_bytes, int nsteps, int sub,
                                             const float *fq, bool active, const float *__restrict__ ext = nullptr) {
     constexpr int NA = 16 / LPR;
@@ -343,11 +351,11 @@ __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_byte
                 uint32_t ws[NA / 2];
                 if constexpr (NA == 16) {
                     const uint4 *r = reinterpret_cast<const uint4 *>(row_bytes + 2 * base);
-                    const uint4 w0 = __ldg(r), w1 = __ldg(r + 1);
+                    const uint4 w0 = ld_row<SMEM>(r), w1 = ld_row<SMEM>(r + 1);
                     ws[0] = w0.x; ws[1] = w0.y; ws[2] = w0.z; ws[3] = w0.w;
                     ws[4] = w1.x; ws[5] = w1.y; ws[6] = w1.z; ws[7] = w1.w;
                 } else {
-                    const uint2 w = __ldg(reinterpret_cast<const uint2 *>(row_bytes + 2 * base));
+                    const uint2 w = ld_row<SMEM>(reinterpret_cast<const uint2 *>(row_bytes + 2 * base));
                     ws[0] = w.x; ws[1] = w.y;
                 }
 #pragma unroll
@@ -360,10 +368,10 @@ __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_byte
                 static_assert(NA == 4 || NA == 16, "SQ8 engine supports 1 or 4 lanes per row");
                 uint32_t ws[NA / 4];
                 if constexpr (NA == 16) {
-                    const uint4 w = __ldg(reinterpret_cast<const uint4 *>(row_bytes + base));
+                    const uint4 w = ld_row<SMEM>(reinterpret_cast<const uint4 *>(row_bytes + base));
                     ws[0] = w.x; ws[1] = w.y; ws[2] = w.z; ws[3] = w.w;
                 } else {
-                    ws[0] = __ldg(reinterpret_cast<const uint32_t *>(row_bytes + base));
+                    ws[0] = ld_row<SMEM>(reinterpret_cast<const uint32_t *>(row_bytes + base));
                 }
                 const float *mi = ext + base, *dif = ext + 16 * nsteps + base;
 #pragma unroll
@@ -373,13 +381,13 @@ __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_byte
                 }
             } else if constexpr (KIND == K_E5M2) {
                 if constexpr (NA == 16) {
-                    uint4 w = __ldg(reinterpret_cast<const uint4 *>(row_bytes + base));
+                    uint4 w = ld_row<SMEM>(reinterpret_cast<const uint4 *>(row_bytes + base));
                     uint32_t ws[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
                     for (int i = 0; i < NA; ++i) y[i] = f32_of_e5m2(ws[i >> 2] >> (8 * (i & 3)));
                 } else {
                     static_assert(NA == 4 || NA == 16, "E5M2 engine supports 1 or 4 lanes per row");
-                    uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(row_bytes + base));
+                    uint32_t w = ld_row<SMEM>(reinterpret_cast<const uint32_t *>(row_bytes + base));
 #pragma unroll
                     for (int i = 0; i < NA; ++i) y[i] = f32_of_e5m2(w >> (8 * i));
                 }
@@ -387,7 +395,7 @@ __device__ __forceinline__ float float_dist(const uint8_t *__restrict__ row_byte
                 const float4 *r4 = reinterpret_cast<const float4 *>(row_bytes) + (base >> 2);
 #pragma unroll
                 for (int i = 0; i < NA / 4; ++i) {
-                    float4 v = __ldg(r4 + i);
+                    float4 v = ld_row<SMEM>(r4 + i);
                     y[4 * i] = v.x; y[4 * i + 1] = v.y; y[4 * i + 2] = v.z; y[4 * i + 3] = v.w;
                 }
             }

@@ -39,7 +39,8 @@ constexpr int kSpeculateRow = 2;     // tuning.prefetch bit: load the predicted 
 constexpr int kPrefetchNeighbours = 4;  // tuning.prefetch bit: L1 prefetch of each neighbour's codes
                                         // before its visited check
 constexpr int kNoStageCodes = 8;     // tuning.prefetch bit: do not stage neighbour code rows in shared
-                                     // memory during the visited check (SQ kinds, rows <= 128 bytes)
+                                     // memory during the visited check (integer kinds with rows of at
+                                     // most 128 bytes; FP16, BF16, E5M2, SQ8 rows of at most 256)
 constexpr int kNoBatchOrder = 16;    // tuning.prefetch bit: run large batches in index order instead of
                                      // sorted by their principal-direction projection
 constexpr int kOrderBins = 2048;     // bins of that sort

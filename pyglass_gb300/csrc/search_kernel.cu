@@ -674,7 +674,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             r1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
         }
         int m = 0;
-        const bool staged = IsIntKind<KIND>::value && L.stage_row > 0;
+        const bool staged = L.stage_row > 0;
         for (int c0 = 0; c0 < ix.K; c0 += 32) {
             const int v = c0 == 0 ? r0 : r1;
             const unsigned endm = __ballot_sync(kFull, v == -1);
@@ -707,9 +707,15 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
                 // distance of this lane's own neighbour from the staged row (one lane per row)
                 cp_async_wait_all();
                 if (fresh) {
-                    const int32_t part = sq_partial_row<KIND, METRIC>(reinterpret_cast<const uint4 *>(srow),
-                                                                      L.stage_row >> 4, w.qc);
-                    w.cand_key[at] = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
+                    if constexpr (IsIntKind<KIND>::value) {
+                        const int32_t part = sq_partial_row<KIND, METRIC>(reinterpret_cast<const uint4 *>(srow),
+                                                                          L.stage_row >> 4, w.qc);
+                        w.cand_key[at] = key_of(sq_finish<KIND, METRIC, 1>(part, qsq));
+                    } else {
+                        // the float engine with one lane per row, reading the staged row
+                        w.cand_key[at] = key_of(float_dist<KIND, METRIC, 1, true>(srow, ix.dalign >> 4, 0, w.fq, true,
+                                                                                ix.sq8p));
+                    }
                 }
             }
             if (fresh) w.cand_id[at] = v;
@@ -1032,8 +1038,12 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     off = up(off, 16);
     L->stage = off;
     L->stage_row = 0;
-    if ((ix.kind == K_SQ4U || ix.kind == K_SQ8U || ix.kind == K_SQ2U || ix.kind == K_SQ4UA || ix.kind == K_SQ1) &&
-        !(prefetch & kNoStageCodes) && ix.csize <= 128 &&
+    // integer rows up to 128 bytes; float rows (FP16, BF16, E5M2, SQ8) up to 256 bytes, whose kernels are
+    // register-limited to fewer resident warps anyway
+    const bool int_kind = ix.kind == K_SQ4U || ix.kind == K_SQ8U || ix.kind == K_SQ2U || ix.kind == K_SQ4UA ||
+                          ix.kind == K_SQ1;
+    const bool small_float = ix.kind == K_FP16 || ix.kind == K_BF16 || ix.kind == K_E5M2 || ix.kind == K_SQ8;
+    if ((int_kind || small_float) && !(prefetch & kNoStageCodes) && ix.csize <= (int_kind ? 128 : 256) &&
         ix.csize % 16 == 0) {
         L->stage_row = ix.csize;
         off += 32 * ix.csize;
