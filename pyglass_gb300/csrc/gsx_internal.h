@@ -40,7 +40,7 @@ constexpr int kPrefetchNeighbours = 4;  // tuning.prefetch bit: L1 prefetch of e
                                         // before its visited check
 constexpr int kNoStageCodes = 8;     // tuning.prefetch bit: do not stage neighbour code rows in shared
                                      // memory during the visited check (integer kinds with rows of at
-                                     // most 128 bytes; FP16, BF16, E5M2, SQ8 rows of at most 256)
+                                     // most 128 bytes; E5M2 rows of at most 256)
 constexpr int kNoBatchOrder = 16;    // tuning.prefetch bit: run large batches in index order instead of
                                      // sorted by their principal-direction projection
 constexpr int kOrderBins = 2048;     // bins of that sort
