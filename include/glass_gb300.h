@@ -147,12 +147,13 @@ typedef struct {
     int32_t lanes_per_row;    /* lanes cooperating on one code row (SQ kinds) */
     int32_t prefetch;         /* bit 4: run batches larger than one wave of resident warps in index
                                  order instead of sorted along the base data's principal
-                                 direction (the order never changes a result); bit 3: do not stage neighbour code rows in shared memory during
-                                 the visited check (staging applies to SQ8U/SQ4U rows of at most
-                                 128 bytes); bit 2: prefetch each neighbour's code row into L1
-                                 before its visited check (unstaged rows); bit 1: load the
-                                 predicted next adjacency row during the merge; bit 0: also
-                                 prefetch that row's code rows */
+                                 direction (the order never changes a result); bit 3: do not
+                                 stage neighbour code rows in shared memory during the visited
+                                 check (staging applies to the integer kinds' rows of at most 128
+                                 bytes and E5M2 rows of at most 256); bit 2: prefetch each
+                                 neighbour's code row into L1 before its visited check (unstaged
+                                 rows); bit 1: load the predicted next adjacency row during the
+                                 merge; bit 0: also prefetch that row's code rows */
     int32_t spill_bits;       /* log2 of the slots of each warp's global visited table (4 bytes a
                                  slot; 7..20, 0 = sized from the visit counts seen) */
 } gsx_tuning;
