@@ -290,12 +290,15 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                     float v[32];
                     const uint32_t col0 = (uint32_t)(ab * kTN + half * (kTN / 2) + c * 32);
                     tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + col0, v);
-                    float dmin = __int_as_float(0x7f800000);
+                    // four independent partial minima keep the dependency chain short
+                    float m4[4] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000),
+                                   __int_as_float(0x7f800000)};
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         v[j] = fmaf(P.neg_scale, v[j], b[j]);
-                        dmin = fminf(dmin, v[j]);
+                        m4[j & 3] = fminf(m4[j & 3], v[j]);
                     }
+                    const float dmin = fminf(fminf(m4[0], m4[1]), fminf(m4[2], m4[3]));
                     if (!(dmin < thr)) continue;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
