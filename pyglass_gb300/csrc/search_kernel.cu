@@ -217,17 +217,20 @@ __device__ __forceinline__ void migrate_visited(WarpState &w, int lane, bool &ba
 }
 
 // merge() for at most 32 surviving candidates (cand_{key,id}[0..ns), arrival order) and a pool of
-// at most 128 entries, in registers.  Candidate j (lane j): rank_j among the candidates, ub_j =
-// pool entries with key <= key_j, found from the last keys of the pool's 4-entry groups (one
-// ballot per candidate) and one 16-byte read of its group; slot_j = ub_j + rank_j.  Pool entry p
-// moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).  Everything that
-// moves is read first, then written once; whatever lands at cap or beyond is dropped.
+// at most 32*GS entries (GS = 4 or 8), in registers.  Candidate j (lane j): rank_j among the
+// candidates, ub_j = pool entries with key <= key_j, found from the last keys of the pool's
+// GS-entry groups (one ballot per candidate) and one read of its group; slot_j = ub_j + rank_j.
+// Pool entry p moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).  The
+// entries from the first candidate's slot up move in blocks of 128 from the top down: a block is
+// read whole, then written, and its entries only move up into blocks already read; whatever lands
+// at cap or beyond is dropped.
+template <int GS>
 __device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &lb, int m, int ns, int lane) {
     const bool has = lane < ns;
     const uint32_t kj = has ? w.cand_key[lane] : 0xffffffffu;
     const int32_t ij = has ? w.cand_id[lane] : 0;
-    const bool full = 4 * lane + 3 < S;
-    const uint32_t piv = full ? w.pkey[4 * lane + 3] : 0u;
+    const bool full = GS * lane + GS - 1 < S;
+    const uint32_t piv = full ? w.pkey[GS * lane + GS - 1] : 0u;
     int rank = 0, grp = 0;
     for (int i = 0; i < ns; ++i) {
         const uint32_t ki = __shfl_sync(kFull, kj, i);
@@ -237,42 +240,51 @@ __device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &
     }
     int ub = 0x7fffffff;  // lanes without a candidate
     if (has) {
-        // the group's four keys: 4*grp + 3 < capacity rounded up to 32, so the read stays in the pool
-        const int g0 = 4 * grp;
-        const uint4 gk = *reinterpret_cast<const uint4 *>(w.pkey + g0);
-        ub = g0 + (int)(g0 < S && gk.x <= kj) + (int)(g0 + 1 < S && gk.y <= kj) + (int)(g0 + 2 < S && gk.z <= kj) +
-             (int)(g0 + 3 < S && gk.w <= kj);
+        // the group's keys: GS*grp + GS-1 < capacity rounded up to 32, so the reads stay in the pool
+        const int g0 = GS * grp;
+        int c = 0;
+#pragma unroll
+        for (int h = 0; h < GS / 4; ++h) {
+            const uint4 gk = *reinterpret_cast<const uint4 *>(w.pkey + g0 + 4 * h);
+            const int b0 = g0 + 4 * h;
+            c += (int)(b0 < S && gk.x <= kj) + (int)(b0 + 1 < S && gk.y <= kj) + (int)(b0 + 2 < S && gk.z <= kj) +
+                 (int)(b0 + 3 < S && gk.w <= kj);
+        }
+        ub = g0 + c;
     }
     const int slot = has ? ub + rank : 0x7fffffff;
     const bool acc = has && slot < cap;
     // the rank-0 candidate always fits (its key is below the last entry of a full pool)
     const int lo = (int)__reduce_min_sync(kFull, acc ? (unsigned)slot : 0x7fffffffu);
-    // pool entries in [lo, S) (S <= 128: at most four per lane) and how far each moves
-    uint32_t pk[4];
-    int32_t pi[4];
-    int pp[4], sh[4];
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        pp[t] = lo + lane + 32 * t;
-        sh[t] = 0;
-        const bool in = pp[t] < S;
-        pk[t] = in ? w.pkey[pp[t]] : 0u;
-        pi[t] = in ? w.pid[pp[t]] : 0;
-    }
-    for (int i = 0; i < ns; ++i) {
-        const int ui = __shfl_sync(kFull, ub, i);
-#pragma unroll
-        for (int t = 0; t < 4; ++t) sh[t] += ui <= pp[t];
-    }
     const int sl = __popc(__ballot_sync(kFull, has && ub <= lb));
-    __syncwarp();
+    // pool entries in [lo, S), 128 at a time from the top (four per lane) and how far each moves
+    for (int blk = S > lo ? (S - 1 - lo) >> 7 : -1; blk >= 0; --blk) {
+        uint32_t pk[4];
+        int32_t pi[4];
+        int pp[4], sh[4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        const int q = pp[t] + sh[t];
-        if (pp[t] < S && sh[t] > 0 && q < cap) {
-            w.pkey[q] = pk[t];
-            w.pid[q] = pi[t];
+        for (int t = 0; t < 4; ++t) {
+            pp[t] = lo + 128 * blk + lane + 32 * t;
+            sh[t] = 0;
+            const bool in = pp[t] < S;
+            pk[t] = in ? w.pkey[pp[t]] : 0u;
+            pi[t] = in ? w.pid[pp[t]] : 0;
         }
+        for (int i = 0; i < ns; ++i) {
+            const int ui = __shfl_sync(kFull, ub, i);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) sh[t] += ui <= pp[t];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int q = pp[t] + sh[t];
+            if (pp[t] < S && sh[t] > 0 && q < cap) {
+                w.pkey[q] = pk[t];
+                w.pid[q] = pi[t];
+            }
+        }
+        __syncwarp();
     }
     if (acc) {
         w.pkey[slot] = kj;
@@ -327,7 +339,11 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     }
     __syncwarp();
     if (ns <= 32 && S <= 128) {
-        merge_small(w, S, cap, lb, m, ns, lane);
+        merge_small<4>(w, S, cap, lb, m, ns, lane);
+        return;
+    }
+    if (ns <= 32 && S <= 256) {
+        merge_small<8>(w, S, cap, lb, m, ns, lane);
         return;
     }
     int nacc = 0;

@@ -255,3 +255,20 @@ def test_sq1_searcher_needs_ip(gpu):
     graph = gpu.Graph(os.path.join(GOLDEN_DIR, "nsg_d100.glass"))
     with pytest.raises(RuntimeError, match="IP metric only"):
         gpu.Searcher(graph, spec.base(), "L2", "SQ1")
+
+
+@pytest.mark.parametrize("quant,metric,refine", [("SQ4U", "L2", "FP32"), ("FP16", "IP", ""), ("SQ8U", "L2", "")])
+def test_large_pools_match_oracle(gpu, oracle, quant, metric, refine):
+    """Pools of 129..256 entries (ef up to 250; k = 100 with the 1.5x refine gives reorder_k 150): the
+    register merge's two-block path, against the oracle."""
+    s = searcher(gpu, "nsg_d100", quant, metric, refine)
+    o = oracle.Searcher(oracle.Graph(os.path.join(GOLDEN_DIR, "nsg_d100.glass")), spec.base(), metric, quant, refine)
+    q = spec.queries()
+    for ef, k in [(200, 10), (250, 100), (129, 100), (64, 100)]:
+        s.set_ef(ef)
+        o.set_ef(ef)
+        gi, gd = s.batch_search(q, k)
+        oi, od = o.batch_search(q, k)
+        np.testing.assert_array_equal(gi, oi)
+        np.testing.assert_array_equal(gd, od)
+        assert s.get_last_search_dist_cmps() == o.get_last_search_dist_cmps()
