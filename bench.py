@@ -211,7 +211,7 @@ def serving_leg(glass, s, queries):
     """Continuous batching under an open-loop Poisson stream: requests of 1..256 queries
     (log-uniform), k in {10, 100}, ef in {32, 64, 128, 256}; the saturation throughput is measured
     with a burst, then p50/p99 request latency at 10%, 50% and 90% of it."""
-    srv = glass.Server(s, capacity=16384, kmax=100, efmax=256, streams=8)
+    srv = glass.Server(s, capacity=65536, kmax=100, efmax=256, streams=16)
     ks, efs = [10, 100], [32, 64, 128, 256]
     mean_size = 256 / np.log(257) - 0.5
     lat, sz, wall = srv.drive_poisson(queries, 2000, 1e7, 1, 256, ks, efs, 7)  # burst: saturation

@@ -197,8 +197,10 @@ typedef struct gsx_server gsx_server;
 
 /* Starts a request loop on searcher s: a dispatcher thread admits queued requests (oldest first)
  * into an arena of max_queries_in_flight device query slots, capped so that the arena takes at
- * most half of the free device memory, and launches each admitted group on one of `streams` CUDA
- * streams, so that groups overlap on the device.  kmax / efmax bound the per-request k and ef.
+ * most half of the free device memory, and launches each admitted group (the oldest requests, up
+ * to max_queries_in_flight / (2 * streams) queries, on one contiguous slot range) on one of
+ * `streams` (1..32) CUDA streams, so that groups overlap on the device.  kmax / efmax bound the
+ * per-request k and ef.
  * While a server runs, the searcher must not be used directly. */
 int gsx_server_create(gsx_searcher *s, int32_t max_queries_in_flight, int32_t kmax, int32_t efmax, int32_t streams,
                       gsx_server **out);

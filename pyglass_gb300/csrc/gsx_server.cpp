@@ -2,11 +2,13 @@
 //
 // Requests (1..n queries, their own k and ef) are queued by gsx_server_submit.  A dispatcher
 // thread admits queued requests, oldest first, into a fixed arena of device query slots (each
-// slot holds one query row, its results and status); admission stops when the arena has no free
-// range for the next request, so device memory bounds the work in flight.  Every admitted group
-// is launched at once on a free stream: copies in, one persistent search launch over the group
-// (its queries addressed through a slot list), copies out, and a host callback that marks the
-// group done.  Groups on different streams overlap on the device, and requests that arrive while
+// slot holds one query row, its results and status); a group of requests takes one contiguous
+// range of slots, and admission stops when the arena has no free range for the next request, so
+// device memory bounds the work in flight.  Every admitted group is launched at once on a free
+// stream: one copy in per array over the group's range, one persistent search launch over the
+// group (its queries addressed through a slot list), one copy out per array, and a host callback
+// that marks the group done, so the dispatcher's work per group does not grow with the number
+// of requests in it.  Groups on different streams overlap on the device, and requests that arrive while
 // others run are admitted as soon as slots and a stream free up.  The search arithmetic is the
 // batched kernel's, so a query's result does not depend on what it ran with.
 #include <cuda_runtime.h>
@@ -52,7 +54,8 @@ struct Request {
 };
 
 struct Group {
-    std::vector<Request *> reqs;
+    std::vector<Request *> reqs;  // consecutive slot ranges starting at slot0
+    int slot0 = -1, nq = 0;
     std::atomic<bool> done{false};
     std::condition_variable *wake = nullptr;
 };
@@ -74,6 +77,11 @@ struct Ranges {
             }
         }
         return -1;
+    }
+    int largest() const {
+        int m = 0;
+        for (const auto &kv : free_) m = std::max(m, kv.second);
+        return m;
     }
     void give(int s, int n) {
         auto it = free_.emplace(s, n).first;
@@ -144,11 +152,11 @@ void finish_group(gsx_server *sv, Group *g) {
                 }
             }
         }
-        sv->ranges.give(r->slot0, r->nq);
         r->state = r->err == GSX_OK ? 2 : 3;
         r->t_done = Clock::now();
         sv->completed_queries += r->nq;
     }
+    sv->ranges.give(g->slot0, g->nq);
     delete g;
 }
 
@@ -163,17 +171,15 @@ int launch_group(gsx_server *sv, Group *g, int si) {
         for (int i = 0; i < r->nq; ++i) {
             sv->hk[r->slot0 + i] = r->k;
             sv->hef[r->slot0 + i] = r->ef;
-            sv->hstatus[r->slot0 + i] = 0;
             order[n++] = r->slot0 + i;
         }
         kmax = std::max(kmax, r->k);
         efmax = std::max(efmax, r->ef);
-        const size_t o = (size_t)r->slot0;
-        GSX_CUDA(cudaMemcpyAsync(sv->dq.as<float>() + o * d, sv->hq + o * d, (size_t)r->nq * d * 4,
-                                 cudaMemcpyHostToDevice, st));
-        GSX_CUDA(cudaMemcpyAsync(sv->dk.as<int32_t>() + o, sv->hk + o, (size_t)r->nq * 4, cudaMemcpyHostToDevice, st));
-        GSX_CUDA(cudaMemcpyAsync(sv->def.as<int32_t>() + o, sv->hef + o, (size_t)r->nq * 4, cudaMemcpyHostToDevice, st));
     }
+    const size_t o = (size_t)g->slot0;
+    GSX_CUDA(cudaMemcpyAsync(sv->dq.as<float>() + o * d, sv->hq + o * d, (size_t)n * d * 4, cudaMemcpyHostToDevice, st));
+    GSX_CUDA(cudaMemcpyAsync(sv->dk.as<int32_t>() + o, sv->hk + o, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+    GSX_CUDA(cudaMemcpyAsync(sv->def.as<int32_t>() + o, sv->hef + o, (size_t)n * 4, cudaMemcpyHostToDevice, st));
     // longest searches first (largest ef, then k), so that the group's tail is short
     std::stable_sort(order, order + n, [&](int32_t a, int32_t b) {
         return sv->hef[a] != sv->hef[b] ? sv->hef[a] > sv->hef[b] : sv->hk[a] > sv->hk[b];
@@ -206,15 +212,11 @@ int launch_group(gsx_server *sv, Group *g, int si) {
         return rc;
     bv.gtab_bits = sbits;
     GSX_CUDA(launch_search(sv->s->ix, bv, cfg, st));
-    for (Request *r : g->reqs) {
-        const size_t o = (size_t)r->slot0;
-        GSX_CUDA(cudaMemcpyAsync(sv->hids + o * sv->kcap, sv->dids.as<int32_t>() + o * sv->kcap,
-                                 (size_t)r->nq * sv->kcap * 4, cudaMemcpyDeviceToHost, st));
-        GSX_CUDA(cudaMemcpyAsync(sv->hdis + o * sv->kcap, sv->ddis.as<float>() + o * sv->kcap,
-                                 (size_t)r->nq * sv->kcap * 4, cudaMemcpyDeviceToHost, st));
-        GSX_CUDA(cudaMemcpyAsync(sv->hstatus + o, sv->dstatus.as<int32_t>() + o, (size_t)r->nq * 4,
-                                 cudaMemcpyDeviceToHost, st));
-    }
+    GSX_CUDA(cudaMemcpyAsync(sv->hids + o * sv->kcap, sv->dids.as<int32_t>() + o * sv->kcap, (size_t)n * sv->kcap * 4,
+                             cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaMemcpyAsync(sv->hdis + o * sv->kcap, sv->ddis.as<float>() + o * sv->kcap, (size_t)n * sv->kcap * 4,
+                             cudaMemcpyDeviceToHost, st));
+    GSX_CUDA(cudaMemcpyAsync(sv->hstatus + o, sv->dstatus.as<int32_t>() + o, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
     GSX_CUDA(cudaLaunchHostFunc(st, on_group_done, g));
     return GSX_OK;
 }
@@ -246,19 +248,29 @@ void dispatcher(gsx_server *sv) {
         if (si >= 0 && !sv->queue.empty()) {
             auto *g = new Group;
             g->wake = &sv->cv;
+            // groups stay small enough that slots cycle quickly (a group's slots free only when its
+            // slowest query is done) and fit the largest free range; FIFO, no overtaking
+            const int room = std::min(sv->max_group, sv->ranges.largest());
             int gq = 0;
-            while (!sv->queue.empty()) {
-                Request *r = sv->queue.front();
-                // groups stay small enough that slots cycle quickly: a group's slots free only when
-                // its slowest query is done
-                if (gq > 0 && gq + r->nq > sv->max_group) break;
-                const int s0 = sv->ranges.take(r->nq);
-                if (s0 < 0) break;  // wait for slots to free (FIFO: no overtaking)
-                r->slot0 = s0;
-                r->state = 1;
-                g->reqs.push_back(r);
+            size_t nr = 0;
+            for (Request *r : sv->queue) {
+                if (gq + r->nq > room && (gq > 0 || r->nq > sv->ranges.largest())) break;
                 gq += r->nq;
-                sv->queue.pop_front();
+                ++nr;
+                if (gq >= room) break;
+            }
+            if (nr > 0) {
+                g->slot0 = sv->ranges.take(gq);
+                g->nq = gq;
+                int s0 = g->slot0;
+                for (size_t i = 0; i < nr; ++i) {
+                    Request *r = sv->queue.front();
+                    sv->queue.pop_front();
+                    r->slot0 = s0;
+                    r->state = 1;
+                    s0 += r->nq;
+                    g->reqs.push_back(r);
+                }
             }
             if (!g->reqs.empty()) {
                 sv->running[si] = g;
@@ -269,8 +281,8 @@ void dispatcher(gsx_server *sv) {
                     // nothing was left queued on the stream for this group that can complete it
                     cudaStreamSynchronize(sv->streams[si]);
                     sv->running[si] = nullptr;
+                    sv->ranges.give(g->slot0, g->nq);
                     for (Request *r : g->reqs) {
-                        sv->ranges.give(r->slot0, r->nq);
                         r->state = 3;
                         r->err = rc;
                         r->msg = gsx_last_error();
@@ -297,7 +309,7 @@ int gsx_server_create(gsx_searcher *s, int32_t max_queries_in_flight, int32_t km
                       gsx_server **out) {
     if (!s || !out) return fail(GSX_ERR_INVALID, "null argument");
     if (!s->has_data) return fail(GSX_ERR_STATE, "server before set_data");
-    if (max_queries_in_flight <= 0 || kmax <= 0 || efmax <= 0 || streams <= 0 || streams > 16)
+    if (max_queries_in_flight <= 0 || kmax <= 0 || efmax <= 0 || streams <= 0 || streams > 32)
         return fail(GSX_ERR_INVALID, "bad server arguments");
     int rc;
     GSX_CUDA(cudaSetDevice(s->device));

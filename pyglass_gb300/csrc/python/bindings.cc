@@ -406,8 +406,8 @@ PYBIND11_MODULE(_glass, m) {
         .def("memory", &Searcher::memory);
 
     py::class_<Server>(m, "Server")
-        .def(py::init<py::object, int, int, int, int>(), py::arg("searcher"), py::arg("capacity") = 16384,
-             py::arg("kmax") = 100, py::arg("efmax") = 256, py::arg("streams") = 8)
+        .def(py::init<py::object, int, int, int, int>(), py::arg("searcher"), py::arg("capacity") = 65536,
+             py::arg("kmax") = 100, py::arg("efmax") = 256, py::arg("streams") = 16)
         .def("submit", &Server::submit, py::arg("query"), py::arg("k"), py::arg("ef"))
         .def("wait", &Server::wait, py::arg("ticket"), py::arg("nq"), py::arg("k"), py::arg("timeout_ms") = 60000)
         .def("capacity", &Server::capacity)
