@@ -191,6 +191,22 @@ int gsx_searcher_params(const gsx_searcher *s, float *params, int32_t *count);
 int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k,
                   int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream);
 
+/* ---- graph construction ------------------------------------------------------------------- */
+
+/* Builds an NSG (use_ssg = 0) or SSG (use_ssg = 1) graph over N fp32 rows (host memory, row-major)
+ * on the GPU; replaces NSG::Build (glass/nsg/nsg.hpp:55-104) behind Index("NSG" | "SSG", metric,
+ * "FP32", R, L).build(data) (python/bindings.cc:60-87).  The graph is R wide with one entry point
+ * (the row nearest to the centroid); L = 0 means R + 32 and C = R + 100, as in the reference
+ * (nsg.hpp:46-53).  Its kNN graph holds the exact knn_k (<= 64; the reference uses 64) nearest rows
+ * from the tensor-core kNN kernel in place of NN-Descent; reverse links are merged per node in one
+ * step instead of one lock-protected insertion at a time, so the build is deterministic.  Squared
+ * L2 over the fp32 rows (the reference's NSG is L2-only); d <= 128, R <= 256.  knng_out (may be
+ * NULL) receives the N x min(knn_k, N - 1) kNN graph; seconds (may be NULL) receives 6 values: kNN
+ * graph + entry point, link, reverse links, connectivity, total, and the number of nodes attached
+ * by the connectivity pass. */
+int gsx_graph_build_nsg(const float *data, int64_t N, int32_t d, int32_t R, int32_t L, int32_t use_ssg,
+                        int32_t knn_k, int32_t *knng_out, double *seconds, gsx_graph **out);
+
 /* ---- serving: continuous batching over a resident index (no reference counterpart) -------- */
 
 typedef struct gsx_server gsx_server;

@@ -85,6 +85,9 @@ def _oracle_lib():
         lib.go_graph_free.argtypes = [C.POINTER(_GoGraph)]
         lib.go_search.argtypes = [C.POINTER(_GoIndex), _f32p, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                   C.c_int, _i32p, _f32p, _i64p, C.c_int]
+        lib.go_nsg_build.argtypes = [_f32p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                     C.c_int32, _i32p, _i32p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        lib.go_nsg_build.restype = C.c_int
         _lib = lib
     return _lib
 
@@ -203,6 +206,28 @@ class Searcher:
 
     def get_last_search_dist_cmps(self) -> float:
         return float(self.last_cmps.mean()) if self.last_cmps is not None else 0.0
+
+
+def nsg_build(data: np.ndarray, R: int, L: int = 0, ssg: bool = False, knn_k: int = 64, knng=None, ep: int = -1):
+    """The restated NSG / SSG build (oracle/nsg_oracle.c): returns (graph N x R, entry point, kNN
+    graph, nodes attached by the connectivity pass).  knng / ep, when given, replace the oracle's own
+    kNN graph / entry point."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    n, d = data.shape
+    k = min(knn_k, n - 1)
+    kn = np.zeros((n, k), np.int32)
+    kin = None
+    if knng is not None:
+        kin = np.ascontiguousarray(knng, dtype=np.int32)
+        assert kin.shape == (n, k)
+    g = np.zeros((n, R), np.int32)
+    ep_out, att = C.c_int32(), C.c_int32()
+    rc = _oracle_lib().go_nsg_build(data, n, d, R, L, 1 if ssg else 0, knn_k,
+                                    kin.ctypes.data if kin is not None else None, int(ep), kn, g,
+                                    C.byref(ep_out), C.byref(att))
+    if rc != 0:
+        raise RuntimeError(f"oracle NSG build failed ({rc})")
+    return g, ep_out.value, kn, att.value
 
 
 _ref = None

@@ -362,9 +362,10 @@ __global__ void row_norms(const float *__restrict__ x, int64_t n, int d, float *
 }
 
 // One warp per query: exact fp64 distances of the candidates, top k by (distance, id).
+// self_base >= 0: query qi is base row self_base + qi and is left out of its own list.
 __global__ void rescore(const float *__restrict__ base, const float *__restrict__ queries, int nq, int d, int ncand,
                         const int32_t *__restrict__ cand, int ip, int k, int32_t *__restrict__ out_ids,
-                        float *__restrict__ out_dis) {
+                        float *__restrict__ out_dis, int64_t self_base) {
     extern __shared__ unsigned char sm[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int qi = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -374,7 +375,8 @@ __global__ void rescore(const float *__restrict__ base, const float *__restrict_
                   (size_t)wib * ncand;
     const float *q = queries + (size_t)qi * d;
     for (int c = lane; c < ncand; c += 32) {
-        const int32_t n = cand[(size_t)qi * ncand + c];
+        int32_t n = cand[(size_t)qi * ncand + c];
+        if (self_base >= 0 && n == self_base + qi) n = -1;
         double s = 0;
         if (n >= 0) {
             // four independent fp64 chains over dimensions j = 4i + t (exact for integer-valued data;
@@ -414,8 +416,16 @@ __global__ void rescore(const float *__restrict__ base, const float *__restrict_
         }
         if (rank < k) {
             out_ids[(size_t)qi * k + rank] = ic;
-            out_dis[(size_t)qi * k + rank] = (float)dc;
+            if (out_dis) out_dis[(size_t)qi * k + rank] = (float)dc;
         }
+    }
+    // fewer than k candidates: the rest of the row is empty
+    int nvalid = 0;
+    for (int c = lane; c < ncand; c += 32) nvalid += id[c] >= 0;
+    for (int o = 16; o; o >>= 1) nvalid += __shfl_xor_sync(0xffffffffu, nvalid, o);
+    for (int r = nvalid + lane; r < k; r += 32) {
+        out_ids[(size_t)qi * k + r] = -1;
+        if (out_dis) out_dis[(size_t)qi * k + r] = __int_as_float(0x7f800000);
     }
 }
 
@@ -449,14 +459,19 @@ int encode_map(CUtensorMap *m, void *ptr, int64_t rows, int dp, int box_rows) {
 
 using namespace gsx;
 
-extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k,
-                             int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream) {
-    if (!d_base || !d_queries || !d_ids || !d_dis || N <= 0 || nq <= 0 || d <= 0)
-        return fail(GSX_ERR_INVALID, "bad arguments");
-    if (k <= 0 || k > kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", kCand);
+namespace gsx {
+
+// Top k of every query over the base set by (distance, id) from the tensor-core candidate lists.
+// The base is split into at least min_chunks chunks, and each 64-column half of a chunk keeps its
+// kCand best candidates, so the result is exact unless more than kCand of a query's k + 1 nearest
+// rows fall into one half-chunk (k <= kCand is always exact).  self_base >= 0 leaves base row
+// self_base + qi out of query qi's list (kNN graph of the base set).
+int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k, int32_t ip,
+               int min_chunks, int64_t self_base, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, cudaStream_t st) {
+    if (!d_base || !d_queries || !d_ids || N <= 0 || nq <= 0 || d <= 0) return fail(GSX_ERR_INVALID, "bad arguments");
+    if (k <= 0 || k > 4 * kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", 4 * kCand);
     if (d > 128) return fail(GSX_ERR_UNSUPPORTED, "exact kNN supports d <= 128");
     if (N > (int64_t)INT32_MAX) return fail(GSX_ERR_INVALID, "N too large");
-    cudaStream_t st = (cudaStream_t)stream;
     const int dp = 128;  // two 64-element K blocks
     DevBuf xh, xl, qh, ql, xn, bias, cand, cand_d, cnt;
     int rc;
@@ -484,7 +499,7 @@ extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const fl
     P.n_mt = (nq + kTM - 1) / kTM;
     P.n_tiles = (int)((N + kTN - 1) / kTN);
     // chunks so that units cover about four waves of the SMs
-    int chunks = std::max(1, (4 * nsm + P.n_mt - 1) / P.n_mt);
+    int chunks = std::max(min_chunks, (4 * nsm + P.n_mt - 1) / P.n_mt);
     chunks = std::min(std::min(chunks, P.n_tiles), 16);  // at most 512 candidates per query
     P.tiles_per_chunk = (P.n_tiles + chunks - 1) / chunks;
     P.n_chunks = (P.n_tiles + P.tiles_per_chunk - 1) / P.tiles_per_chunk;
@@ -514,11 +529,20 @@ extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const fl
     if (rs_smem > 227 * 1024) return fail(GSX_ERR_UNSUPPORTED, "too many candidate lists");
     GSX_CUDA(cudaFuncSetAttribute(rescore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem));
     rescore<<<(nq + wpb - 1) / wpb, wpb * 32, rs_smem, st>>>(d_base, d_queries, nq, d, (int)ncand, P.cand, P.ip, k,
-                                                             d_ids, d_dis);
+                                                             d_ids, d_dis, self_base);
     GSX_CUDA(cudaGetLastError());
     unsigned err = 0;
     GSX_CUDA(cudaMemcpyAsync(&err, cnt.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
     GSX_CUDA(cudaStreamSynchronize(st));
     if (err) return fail(GSX_ERR_TIMEOUT, "tensor-core kNN kernel gave up waiting on a pipeline barrier");
     return GSX_OK;
+}
+
+}  // namespace gsx
+
+extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k,
+                             int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream) {
+    if (!d_dis) return fail(GSX_ERR_INVALID, "bad arguments");
+    if (k > kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", kCand);
+    return knn_select(d_base, N, d, d_queries, nq, k, ip, 1, -1, d_ids, d_dis, exact_inputs, (cudaStream_t)stream);
 }

@@ -5,6 +5,7 @@
 #include <pybind11/numpy.h>
 #include <pybind11/pybind11.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <memory>
 #include <stdexcept>
@@ -265,6 +266,71 @@ struct Searcher {
 };
 
 // The serving loop (gsx_server_*): submit returns a ticket, wait returns (ids, dis, latency_ms).
+// Index (python/bindings.cc:60-87): "NSG" and "SSG" over FP32 rows build on the GPU
+// (gsx_graph_build_nsg); other index types and build quantizers raise.
+struct Index {
+    std::string type;
+    int R = 32, L = 0;
+    double secs[6] = {0, 0, 0, 0, 0, 0};
+    py::object knng = py::none();
+
+    Index(const std::string &index_type, const std::string &metric, const std::string &quant, int R_, int L_)
+        : type(index_type), R(R_), L(L_) {
+        if (index_type != "NSG" && index_type != "SSG")
+            throw std::runtime_error("glass-gb300: index type " + index_type +
+                                     " is not built on the GPU (NSG and SSG are)");
+        if (metric != "L2" && metric != "IP")
+            throw std::runtime_error("glass-gb300: unknown metric " + metric);
+        if (quant != "FP32")
+            throw std::runtime_error("glass-gb300: the GPU graph build computes FP32 distances (quant \"FP32\")");
+    }
+    Graph *build(py::object input, int knn_k, bool keep_knn) {
+        f32arr items(input);
+        size_t rows = 0, features = 0;
+        shape_of(items.request(), &rows, &features);
+        const int kk = (int)std::min<size_t>((size_t)knn_k, rows > 1 ? rows - 1 : 1);
+        py::array_t<int32_t> kn;
+        int32_t *kp = nullptr;
+        if (keep_knn) {
+            kn = py::array_t<int32_t>({(py::ssize_t)rows, (py::ssize_t)kk});
+            kp = kn.mutable_data();
+        }
+        auto *G = new Graph;
+        int rc;
+        {
+            py::gil_scoped_release rel;
+            rc = gsx_graph_build_nsg(items.data(), (int64_t)rows, (int32_t)features, R, L, type == "SSG" ? 1 : 0, knn_k, kp,
+                                     secs, &G->g);
+        }
+        if (rc != GSX_OK) {
+            delete G;
+            check(rc);
+        }
+        knng = keep_knn ? py::object(kn) : py::object(py::none());
+        return G;
+    }
+    double get_construction_time() const { return secs[4]; }
+    py::dict stages() const {
+        py::dict d;
+        d["knn_graph_s"] = secs[0];
+        d["link_s"] = secs[1];
+        d["reverse_s"] = secs[2];
+        d["connect_s"] = secs[3];
+        d["total_s"] = secs[4];
+        d["attached"] = (int64_t)secs[5];
+        return d;
+    }
+};
+
+// build_graph (python/bindings.cc:231-237)
+double build_graph(const std::string &index_type, py::object input, const std::string &graph_file,
+                   const std::string &metric, const std::string &quant, int R, int L) {
+    Index index(index_type, metric, quant, R, L);
+    std::unique_ptr<Graph> g(index.build(input, 64, false));
+    g->save(graph_file);
+    return index.get_construction_time();
+}
+
 struct Server {
     gsx_server *sv = nullptr;
     int32_t dim = 0;
@@ -404,6 +470,18 @@ PYBIND11_MODULE(_glass, m) {
         .def("set_tuning", &Searcher::set_tuning, py::arg("warps_per_block") = 0, py::arg("table_bits") = 0,
              py::arg("lanes_per_row") = 0, py::arg("prefetch") = 2, py::arg("spill_bits") = 0)
         .def("memory", &Searcher::memory);
+
+    py::class_<Index>(m, "Index")
+        .def(py::init<const std::string &, const std::string &, const std::string &, int, int>(), py::arg("index_type"),
+             py::arg("metric"), py::arg("quant") = "FP32", py::arg("R") = 32, py::arg("L") = 0)
+        .def("build", &Index::build, py::arg("data"), py::arg("knn_k") = 64, py::arg("keep_knn") = false,
+             py::return_value_policy::take_ownership)
+        .def("get_construction_time", &Index::get_construction_time)
+        .def("stages", &Index::stages)
+        .def_readonly("knn_graph", &Index::knng);
+
+    m.def("build_graph", &build_graph, py::arg("index_type"), py::arg("input"), py::arg("graph_file"),
+          py::arg("metric"), py::arg("quant") = "FP32", py::arg("R") = 32, py::arg("L") = 0);
 
     py::class_<Server>(m, "Server")
         .def(py::init<py::object, int, int, int, int>(), py::arg("searcher"), py::arg("capacity") = 65536,
