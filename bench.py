@@ -230,6 +230,24 @@ def serving_leg(glass, s, queries):
             "at": "50% of saturation"}
 
 
+def graph_build_leg(glass, base, queries, gt, meta, ef, ref_recall):
+    """NSG build of the workload's base set on the GPU (R 32, L 50, as the reference built the
+    searched graph), then the same SQ4U + FP32 search on it at the headline ef."""
+    idx = glass.Index("NSG", "L2", "FP32", 32, 50)
+    t = time.perf_counter()
+    g = idx.build(base)
+    wall = time.perf_counter() - t
+    s2 = glass.Searcher(g, base, "L2", "SQ4U", "FP32")
+    s2.set_ef(ef)
+    ids, _ = s2.batch_search(queries, K)
+    out = {"index": "NSG R=32 L=50, FP32 distances, exact 64-NN graph", "seconds": wall, "stages": idx.stages(),
+           "recall@10_at_ef": {"ef": ef, "gpu_built": recall(ids, gt), "reference_built": ref_recall},
+           "reference_cpu_seconds": meta.get("build_seconds"),
+           "reference_cpu_note": "the reference's NSG builder (NN-Descent, SQ8U distances) on 8 x86 cores"}
+    del s2, g
+    return out
+
+
 def replica_throughput(local_seconds, nq, steps, world, dist=None, device="cpu"):
     """Whole-job QPS of `world` replicas that each searched nq queries per step: the slowest
     rank's time bounds the job (max over ranks; no data is exchanged)."""
@@ -416,6 +434,7 @@ def run_gpu(a):
              "p99_ms": float(np.percentile(lat_ms, 99)), "queries": int(lat_ms.size)}
 
     serving = serving_leg(glass, s, queries)
+    build = graph_build_leg(glass, base, queries, gt, meta, a.ef, rec) if rank == 0 else None
 
     if rank == 0:
         cb, _ = cpu_baseline(base, queries, a.ef, min(a.cpu_sample, nq))
@@ -432,7 +451,7 @@ def run_gpu(a):
                          "avg_expansions": float(x.mean())},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": a.steps, "clocks": clk.summary(),
             "plain_per_query": plain, "batched_over_plain": value / world / plain["qps"], "sweep": sweep,
-            "ground_truth": gt_info, "serving": serving,
+            "ground_truth": gt_info, "serving": serving, "graph_build": build,
         }
         print(json.dumps(line))
     if dist:

@@ -61,6 +61,8 @@ int gsx_graph_save(const gsx_graph *g, const char *filename);
 int gsx_graph_info(const gsx_graph *g, int32_t *N, int32_t *K, int32_t *nep, int32_t *has_hnsw);
 /* Copies the adjacency (N*K int32) out. */
 int gsx_graph_adjacency(const gsx_graph *g, int32_t *adj_out);
+/* Copies the entry points (nep int32, Graph::eps, graph.hpp:37) out. */
+int gsx_graph_eps(const gsx_graph *g, int32_t *eps_out);
 void gsx_graph_destroy(gsx_graph *g);
 
 /* ---- searchers: GraphSearcherBase (glass/searcher/searcher_base.hpp:7-19) ---------------- */

@@ -580,6 +580,12 @@ int gsx_graph_adjacency(const gsx_graph *g, int32_t *adj_out) {
     return GSX_OK;
 }
 
+int gsx_graph_eps(const gsx_graph *g, int32_t *eps_out) {
+    if (!g || !eps_out) return fail(GSX_ERR_INVALID, "null argument");
+    std::memcpy(eps_out, g->g.eps.data(), g->g.eps.size() * 4);
+    return GSX_OK;
+}
+
 void gsx_graph_destroy(gsx_graph *g) { delete g; }
 
 int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quantizer, const char *refine_quant,
