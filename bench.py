@@ -44,6 +44,8 @@ def args_():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--cpu-sample", type=int, default=2000, help="queries per CPU-baseline step")
     p.add_argument("--gt-only", action="store_true", help="only the tensor-core ground truth (for ncu captures)")
+    p.add_argument("--build-only", type=int, default=0, metavar="ROWS",
+                   help="only the GPU NSG build of the first ROWS base rows (for ncu launch lists)")
     p.add_argument("--profile", action="store_true",
                    help="only the warm-up and timed device launches (default tuning), for ncu captures")
     return p.parse_args()
@@ -324,6 +326,12 @@ def run_gpu(a):
 
     base, queries, meta = load_workload()
     nq, d = queries.shape
+    if a.build_only:
+        idx = glass.Index("NSG", "L2", "FP32", 32, 50)
+        t = time.perf_counter()
+        idx.build(base[: a.build_only])
+        print(json.dumps({"build_only": a.build_only, "seconds": time.perf_counter() - t, "stages": idx.stages()}))
+        return
     if a.gt_only:
         bt = torch.from_numpy(base).cuda()
         qt = torch.from_numpy(queries).cuda()

@@ -2,8 +2,8 @@
  * the checker of the GPU build (pyglass_gb300/csrc/build_kernel.cu); never part of the product.
  *
  * It follows the reference's builder glass/nsg/nsg.hpp stage by stage:
- *   - kNN graph: exact by brute force (fp64 squared L2 in four chains over j & 3, (distance, id)
- *     order, the row itself left out) where the reference runs NN-Descent (nsg/nndescent.hpp);
+ *   - kNN graph: exact by brute force ((distance, id) order over the fp32 distance below, the row
+ *     itself left out) where the reference runs NN-Descent (nsg/nndescent.hpp);
  *   - entry point: the row nearest to the centroid (nsg.hpp:106-127);
  *   - link: search_on_graph over the kNN graph from the entry point with a LinearPool of L entries
  *     (nsg.hpp:129-158, neighbor.hpp:320-433), sync_prune over the C = R + 100 nearest evaluated
@@ -28,15 +28,6 @@ static float l2f(const float *a, const float *b, int d) {
     for (int j = 0; j < d; ++j) {
         const float t = a[j] - b[j];
         c[j & 3] = fmaf(t, t, c[j & 3]);
-    }
-    return (c[0] + c[1]) + (c[2] + c[3]);
-}
-
-static double l2d(const float *a, const float *b, int d) {
-    double c[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int j = 0; j < d; ++j) {
-        const double t = (double)a[j] - (double)b[j];
-        c[j & 3] += t * t;
     }
     return (c[0] + c[1]) + (c[2] + c[3]);
 }
@@ -155,7 +146,7 @@ int go_nsg_build(const float *x, int64_t N, int d, int R, int L, int ssg, int kn
                 int64_t n = 0;
                 for (int64_t r = 0; r < N; ++r) {
                     if (r == q) continue;
-                    all[n].d = l2d(x + q * d, x + r * d, d);
+                    all[n].d = (double)l2f(x + r * d, x + q * d, d);
                     all[n].id = (int32_t)r;
                     ++n;
                 }

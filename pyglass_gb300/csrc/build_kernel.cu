@@ -2,8 +2,9 @@
 // Python as Index("NSG" | "SSG", ...).build(data), python/bindings.cc:60-87).
 //
 // Stages, all writing the glass graph layout (N x R int32, -1 padded, one entry point):
-//   1. kNN graph of the base set (knn_k neighbours, self excluded) from the tensor-core kNN kernel
-//      (the reference builds it with NN-Descent, nsg/nndescent.hpp; an exact graph is its limit).
+//   1. kNN graph of the base set (knn_k neighbours, self excluded) from the tensor-core kNN kernel,
+//      its candidates ranked by the fp32 distance below (the reference builds the graph with
+//      NN-Descent, nsg/nndescent.hpp; the exact graph is its limit).
 //   2. Entry point: the row nearest to the centroid (nsg.hpp:106-127).
 //   3. Link (nsg.hpp:160-246): one warp per node runs the reference's search over the kNN graph
 //      from the entry point (LinearPool of L entries, nsg.hpp:129-158), keeps the C = R + 100
@@ -33,7 +34,8 @@
 namespace gsx {
 
 int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k, int32_t ip,
-               int min_chunks, int64_t self_base, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, cudaStream_t st);
+               int min_chunks, int64_t self_base, int fp32_l2, int32_t *d_ids, float *d_dis, int32_t *exact_inputs,
+               cudaStream_t st);
 
 namespace {
 
@@ -792,8 +794,8 @@ extern "C" int gsx_graph_build_nsg(const float *data, int64_t N, int32_t d, int3
     const int64_t qblock = 1 << 18;
     for (int64_t q0 = 0; q0 < N; q0 += qblock) {
         const int nq = (int)std::min<int64_t>(qblock, N - q0);
-        if ((rc = knn_select(x.as<float>(), N, d, x.as<float>() + q0 * d, nq, K, 0, 16, q0, knng.as<int32_t>() + q0 * K,
-                             nullptr, nullptr, st)))
+        if ((rc = knn_select(x.as<float>(), N, d, x.as<float>() + q0 * d, nq, K, 0, 16, q0, 1,
+                             knng.as<int32_t>() + q0 * K, nullptr, nullptr, st)))
             return rc;
     }
     // 2. entry point

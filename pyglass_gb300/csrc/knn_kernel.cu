@@ -362,23 +362,65 @@ __global__ void row_norms(const float *__restrict__ x, int64_t n, int d, float *
 }
 
 // One warp per query: exact fp64 distances of the candidates, top k by (distance, id).
+// Order-preserving 64-bit key of a distance (-0 taken as +0), so that the ranking below compares
+// integers: GB300's fp64 pipe is a small fraction of its integer and fp32 rate.
+__device__ __forceinline__ unsigned long long dist_key(double s) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(s + 0.0);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// squared L2 in fp32: four fmaf chains over dimensions j = 4i + t, summed (c0 + c1) + (c2 + c3)
+__device__ __forceinline__ float l2_chain(const float *a, const float *b, int d, bool vec4) {
+    float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
+    int j = 0;
+    if (vec4) {
+        for (; j < d; j += 4) {
+            const float4 x = __ldg(reinterpret_cast<const float4 *>(a + j));
+            const float4 y = *reinterpret_cast<const float4 *>(b + j);
+            const float t0 = x.x - y.x, t1 = x.y - y.y, t2 = x.z - y.z, t3 = x.w - y.w;
+            c0 = fmaf(t0, t0, c0);
+            c1 = fmaf(t1, t1, c1);
+            c2 = fmaf(t2, t2, c2);
+            c3 = fmaf(t3, t3, c3);
+        }
+    }
+    for (; j < d; ++j) {
+        const float t = a[j] - b[j];
+        const int c = j & 3;
+        if (c == 0) c0 = fmaf(t, t, c0);
+        else if (c == 1) c1 = fmaf(t, t, c1);
+        else if (c == 2) c2 = fmaf(t, t, c2);
+        else c3 = fmaf(t, t, c3);
+    }
+    return (c0 + c1) + (c2 + c3);
+}
+
 // self_base >= 0: query qi is base row self_base + qi and is left out of its own list.
+// fp32_l2: the distances are squared L2 in the fp32 order of l2_chain (the graph build's own
+// distance), else exact-ish fp64 (the recall ground truth).
 __global__ void rescore(const float *__restrict__ base, const float *__restrict__ queries, int nq, int d, int ncand,
                         const int32_t *__restrict__ cand, int ip, int k, int32_t *__restrict__ out_ids,
-                        float *__restrict__ out_dis, int64_t self_base) {
+                        float *__restrict__ out_dis, int64_t self_base, int fp32_l2) {
     extern __shared__ unsigned char sm[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int qi = blockIdx.x * (blockDim.x >> 5) + wib;
     if (qi >= nq) return;
+    const int wpb = blockDim.x >> 5;
     double *dd = reinterpret_cast<double *>(sm) + (size_t)wib * ncand;
-    int32_t *id = reinterpret_cast<int32_t *>(reinterpret_cast<double *>(sm) + (size_t)(blockDim.x >> 5) * ncand) +
+    unsigned long long *kk = reinterpret_cast<unsigned long long *>(reinterpret_cast<double *>(sm) + (size_t)wpb * ncand) +
+                             (size_t)wib * ncand;
+    int32_t *id = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned long long *>(sm) + (size_t)2 * wpb * ncand) +
                   (size_t)wib * ncand;
     const float *q = queries + (size_t)qi * d;
+    const bool vec4 =
+        (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(base) | reinterpret_cast<uintptr_t>(queries)) & 15) == 0;
     for (int c = lane; c < ncand; c += 32) {
         int32_t n = cand[(size_t)qi * ncand + c];
         if (self_base >= 0 && n == self_base + qi) n = -1;
         double s = 0;
-        if (n >= 0) {
+        if (n >= 0 && fp32_l2) {
+            s = (double)l2_chain(base + (size_t)n * d, q, d, vec4);
+        } else if (n >= 0) {
             // four independent fp64 chains over dimensions j = 4i + t (exact for integer-valued data;
             // otherwise within a few fp64 ulps of any other order), 16-byte loads when rows allow
             const float *x = base + (size_t)n * d;
@@ -401,18 +443,20 @@ __global__ void rescore(const float *__restrict__ base, const float *__restrict_
             s = ip ? -s : s;
         }
         dd[c] = n >= 0 ? s : 1e300;
+        kk[c] = n >= 0 ? dist_key(s) : ~0ull;
         id[c] = n;
     }
     __syncwarp();
     for (int c = lane; c < ncand; c += 32) {
+        const unsigned long long kc = kk[c];
         const double dc = dd[c];
         const int32_t ic = id[c];
         if (ic < 0) continue;
         int rank = 0;
         for (int o = 0; o < ncand; ++o) {
-            const double x = dd[o];
+            const unsigned long long x = kk[o];
             const int32_t io = id[o];
-            rank += io >= 0 && (x < dc || (x == dc && io < ic));
+            rank += io >= 0 && (x < kc || (x == kc && io < ic));
         }
         if (rank < k) {
             out_ids[(size_t)qi * k + rank] = ic;
@@ -467,7 +511,8 @@ namespace gsx {
 // rows fall into one half-chunk (k <= kCand is always exact).  self_base >= 0 leaves base row
 // self_base + qi out of query qi's list (kNN graph of the base set).
 int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k, int32_t ip,
-               int min_chunks, int64_t self_base, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, cudaStream_t st) {
+               int min_chunks, int64_t self_base, int fp32_l2, int32_t *d_ids, float *d_dis, int32_t *exact_inputs,
+               cudaStream_t st) {
     if (!d_base || !d_queries || !d_ids || N <= 0 || nq <= 0 || d <= 0) return fail(GSX_ERR_INVALID, "bad arguments");
     if (k <= 0 || k > 4 * kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", 4 * kCand);
     if (d > 128) return fail(GSX_ERR_UNSUPPORTED, "exact kNN supports d <= 128");
@@ -525,11 +570,11 @@ int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries
     knn_tc_kernel<<<std::min(units, nsm), kThreads, kSmemBytes, st>>>(mqh, mql, mxh, mxl, P);
     GSX_CUDA(cudaGetLastError());
     const int wpb = 4;
-    const size_t rs_smem = (size_t)wpb * ncand * 12;
+    const size_t rs_smem = (size_t)wpb * ncand * 20;
     if (rs_smem > 227 * 1024) return fail(GSX_ERR_UNSUPPORTED, "too many candidate lists");
     GSX_CUDA(cudaFuncSetAttribute(rescore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem));
     rescore<<<(nq + wpb - 1) / wpb, wpb * 32, rs_smem, st>>>(d_base, d_queries, nq, d, (int)ncand, P.cand, P.ip, k,
-                                                             d_ids, d_dis, self_base);
+                                                             d_ids, d_dis, self_base, fp32_l2);
     GSX_CUDA(cudaGetLastError());
     unsigned err = 0;
     GSX_CUDA(cudaMemcpyAsync(&err, cnt.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
@@ -544,5 +589,5 @@ extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const fl
                              int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream) {
     if (!d_dis) return fail(GSX_ERR_INVALID, "bad arguments");
     if (k > kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", kCand);
-    return knn_select(d_base, N, d, d_queries, nq, k, ip, 1, -1, d_ids, d_dis, exact_inputs, (cudaStream_t)stream);
+    return knn_select(d_base, N, d, d_queries, nq, k, ip, 1, -1, 0, d_ids, d_dis, exact_inputs, (cudaStream_t)stream);
 }

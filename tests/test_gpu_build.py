@@ -69,7 +69,8 @@ def test_float_data_matches_oracle(glass, oracle, tmp_path, kind):
     x = np.random.default_rng(7).standard_normal((4000, 64)).astype(np.float32)
     g, idx = _build(glass, x, kind, 24, 0)
     adj, ep = _adj(glass, g, tmp_path)
-    # the kNN graph is the exact one (fp64 distances, (distance, id) order)
+    # the kNN graph is the exact one (fp32 distances, (distance, id) order; fp64 agrees but for
+    # near-ties)
     x64 = x.astype(np.float64)
     sq = (x64 * x64).sum(1)
     D = sq[:, None] + sq[None, :] - 2 * x64 @ x64.T
@@ -77,8 +78,10 @@ def test_float_data_matches_oracle(glass, oracle, tmp_path, kind):
     rows = np.arange(0, 4000, 7)
     exact = np.stack([np.argsort(D[i], kind="stable")[:64] for i in rows])
     assert np.mean(np.all(idx.knn_graph[rows] == exact, axis=1)) > 0.99
-    # link / reverse / connectivity: bit-identical given the same kNN graph and entry point
-    want, wep, _, watt = pyoracle.nsg_build(x, 24, 0, kind == "SSG", knng=idx.knn_graph, ep=ep)
+    # the oracle's own kNN graph (same fp32 order) equals the GPU's; link / reverse / connectivity
+    # are bit-identical given the same entry point
+    want, wep, wkn, watt = pyoracle.nsg_build(x, 24, 0, kind == "SSG", ep=ep)
+    np.testing.assert_array_equal(idx.knn_graph, wkn)
     assert wep == ep
     np.testing.assert_array_equal(adj, want)
     assert idx.stages()["attached"] == watt
