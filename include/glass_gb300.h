@@ -200,12 +200,14 @@ int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const float *d_quer
  * "FP32", R, L).build(data) (python/bindings.cc:60-87).  The graph is R wide with one entry point
  * (the row nearest to the centroid); L = 0 means R + 32 and C = R + 100, as in the reference
  * (nsg.hpp:46-53).  Its kNN graph holds the exact knn_k (<= 64; the reference uses 64) nearest rows
- * from the tensor-core kNN kernel in place of NN-Descent; reverse links are merged per node in one
- * step instead of one lock-protected insertion at a time, so the build is deterministic.  Squared
+ * by fp32 squared L2 (tensor-core candidates, brute force where they may fall short) in place of
+ * NN-Descent; reverse links are merged per node in one step instead of one lock-protected
+ * insertion at a time, so the build is deterministic.  Squared
  * L2 over the fp32 rows (the reference's NSG is L2-only); d <= 128, R <= 256.  knng_out (may be
- * NULL) receives the N x min(knn_k, N - 1) kNN graph; seconds (may be NULL) receives 6 values: kNN
- * graph + entry point, link, reverse links, connectivity, total, and the number of nodes attached
- * by the connectivity pass. */
+ * NULL) receives the N x min(knn_k, N - 1) kNN graph; seconds (may be NULL) receives 7 values: kNN
+ * graph + entry point, link, reverse links, connectivity, total, the number of nodes attached by
+ * the connectivity pass, and the number of kNN rows redone by brute force (rows whose tensor-core
+ * candidate lists may have cut their neighbours short). */
 int gsx_graph_build_nsg(const float *data, int64_t N, int32_t d, int32_t R, int32_t L, int32_t use_ssg,
                         int32_t knn_k, int32_t *knng_out, double *seconds, gsx_graph **out);
 

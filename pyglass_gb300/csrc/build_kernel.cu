@@ -2,9 +2,10 @@
 // Python as Index("NSG" | "SSG", ...).build(data), python/bindings.cc:60-87).
 //
 // Stages, all writing the glass graph layout (N x R int32, -1 padded, one entry point):
-//   1. kNN graph of the base set (knn_k neighbours, self excluded) from the tensor-core kNN kernel,
-//      its candidates ranked by the fp32 distance below (the reference builds the graph with
-//      NN-Descent, nsg/nndescent.hpp; the exact graph is its limit).
+//   1. Exact kNN graph of the base set (knn_k neighbours, self excluded, by the fp32 distance below):
+//      tensor-core candidate lists, rescored; rows a full list may have cut short are redone by
+//      brute force (the reference builds the graph with NN-Descent, nsg/nndescent.hpp; the exact
+//      graph is its limit).
 //   2. Entry point: the row nearest to the centroid (nsg.hpp:106-127).
 //   3. Link (nsg.hpp:160-246): one warp per node runs the reference's search over the kNN graph
 //      from the entry point (LinearPool of L entries, nsg.hpp:129-158), keeps the C = R + 100
@@ -35,7 +36,7 @@ namespace gsx {
 
 int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k, int32_t ip,
                int min_chunks, int64_t self_base, int fp32_l2, int32_t *d_ids, float *d_dis, int32_t *exact_inputs,
-               cudaStream_t st);
+               int32_t *rechecked, cudaStream_t st);
 
 namespace {
 
@@ -792,11 +793,14 @@ extern "C" int gsx_graph_build_nsg(const float *data, int64_t N, int32_t d, int3
     GSX_CUDA(cudaMemcpyAsync(x.p, data, (size_t)N * d * 4, cudaMemcpyHostToDevice, st));
     // 1. kNN graph, in query blocks that keep the candidate lists near 1 GB
     const int64_t qblock = 1 << 18;
+    int64_t n_re = 0;
     for (int64_t q0 = 0; q0 < N; q0 += qblock) {
         const int nq = (int)std::min<int64_t>(qblock, N - q0);
+        int32_t re = 0;
         if ((rc = knn_select(x.as<float>(), N, d, x.as<float>() + q0 * d, nq, K, 0, 16, q0, 1,
-                             knng.as<int32_t>() + q0 * K, nullptr, nullptr, st)))
+                             knng.as<int32_t>() + q0 * K, nullptr, nullptr, &re, st)))
             return rc;
+        n_re += re;
     }
     // 2. entry point
     if ((rc = sums.ensure((size_t)d * 8)) || (rc = cen.ensure((size_t)d * 4)) || (rc = best.ensure(8))) return rc;
@@ -936,6 +940,7 @@ extern "C" int gsx_graph_build_nsg(const float *data, int64_t N, int32_t d, int3
     if (seconds) {
         for (int i = 0; i < 5; ++i) seconds[i] = t[i];
         seconds[5] = (double)n_att;
+        seconds[6] = (double)n_re;
     }
     *out = gr;
     return GSX_OK;

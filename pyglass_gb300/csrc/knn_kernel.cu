@@ -398,19 +398,25 @@ __device__ __forceinline__ float l2_chain(const float *a, const float *b, int d,
 // self_base >= 0: query qi is base row self_base + qi and is left out of its own list.
 // fp32_l2: the distances are squared L2 in the fp32 order of l2_chain (the graph build's own
 // distance), else exact-ish fp64 (the recall ground truth).
+// recheck (may be null): queries whose top k may miss a row that a full candidate list dropped
+// (its last kept approximate distance not clearly above the k-th distance, approximate distances
+// being the L2 distance minus |q|^2), or that have fewer than k candidates, are appended to
+// recheck[1..] (count in recheck[0]) for the brute-force pass.
 __global__ void rescore(const float *__restrict__ base, const float *__restrict__ queries, int nq, int d, int ncand,
-                        const int32_t *__restrict__ cand, int ip, int k, int32_t *__restrict__ out_ids,
-                        float *__restrict__ out_dis, int64_t self_base, int fp32_l2) {
+                        const int32_t *__restrict__ cand, const float *__restrict__ cand_d, int ip, int k,
+                        int32_t *__restrict__ out_ids, float *__restrict__ out_dis, int64_t self_base, int fp32_l2,
+                        int32_t *__restrict__ recheck) {
     extern __shared__ unsigned char sm[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int qi = blockIdx.x * (blockDim.x >> 5) + wib;
     if (qi >= nq) return;
     const int wpb = blockDim.x >> 5;
-    double *dd = reinterpret_cast<double *>(sm) + (size_t)wib * ncand;
-    unsigned long long *kk = reinterpret_cast<unsigned long long *>(reinterpret_cast<double *>(sm) + (size_t)wpb * ncand) +
-                             (size_t)wib * ncand;
-    int32_t *id = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned long long *>(sm) + (size_t)2 * wpb * ncand) +
-                  (size_t)wib * ncand;
+    const size_t cs = (size_t)ncand + 1;  // per-warp stride: the candidates and one spare slot
+    double *dd = reinterpret_cast<double *>(sm) + (size_t)wib * cs;
+    unsigned long long *kk =
+        reinterpret_cast<unsigned long long *>(reinterpret_cast<double *>(sm) + (size_t)wpb * cs) + (size_t)wib * cs;
+    int32_t *id = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned long long *>(sm) + (size_t)2 * wpb * cs) +
+                  (size_t)wib * cs;
     const float *q = queries + (size_t)qi * d;
     const bool vec4 =
         (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(base) | reinterpret_cast<uintptr_t>(queries)) & 15) == 0;
@@ -462,6 +468,7 @@ __global__ void rescore(const float *__restrict__ base, const float *__restrict_
             out_ids[(size_t)qi * k + rank] = ic;
             if (out_dis) out_dis[(size_t)qi * k + rank] = (float)dc;
         }
+        if (rank == k - 1) dd[ncand] = dc;  // spare slot past this warp's candidates: the k-th distance
     }
     // fewer than k candidates: the rest of the row is empty
     int nvalid = 0;
@@ -470,6 +477,90 @@ __global__ void rescore(const float *__restrict__ base, const float *__restrict_
     for (int r = nvalid + lane; r < k; r += 32) {
         out_ids[(size_t)qi * k + r] = -1;
         if (out_dis) out_dis[(size_t)qi * k + r] = __int_as_float(0x7f800000);
+    }
+    if (recheck) {
+        __syncwarp();
+        bool flag = nvalid < k;
+        if (!flag) {
+            const double kth = dd[ncand];
+            double qn = 0.0;
+            for (int j = 0; j < d; ++j) qn += (double)q[j] * q[j];
+            const double lim = kth - qn + 1e-4 * (qn + fabs(kth)) + 1e-30;
+            for (int l = lane; l < ncand / kCand; l += 32) {
+                const size_t last = (size_t)qi * ncand + (size_t)l * kCand + kCand - 1;
+                flag |= cand[last] >= 0 && (double)cand_d[last] <= lim;
+            }
+        }
+        if (__any_sync(0xffffffffu, flag) && lane == 0) {
+            const int at = atomicAdd(recheck, 1);
+            recheck[1 + at] = qi;
+        }
+    }
+}
+
+// keeps the k smallest (distance, id) pairs of one warp, sorted (k + 1 slots)
+__device__ __forceinline__ void top_insert(float *td, int32_t *ti, int &n, int k, float dist, int32_t id, int lane) {
+    if (n == k && !(dist < td[k - 1] || (dist == td[k - 1] && id < ti[k - 1]))) return;
+    int pos = 0;
+    for (int b = 0; b < n; b += 32) {
+        const int i = b + lane;
+        pos += __popc(__ballot_sync(0xffffffffu, i < n && (td[i] < dist || (td[i] == dist && ti[i] < id))));
+    }
+    for (int top = n; top > pos; top -= 32) {
+        const int i = top - 1 - lane;
+        float a = 0.0f;
+        int32_t b = 0;
+        if (i >= pos) {
+            a = td[i];
+            b = ti[i];
+        }
+        __syncwarp();
+        if (i >= pos) {
+            td[i + 1] = a;
+            ti[i + 1] = b;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        td[pos] = dist;
+        ti[pos] = id;
+    }
+    __syncwarp();
+    if (n < k) ++n;
+}
+
+// Exact top k of listed queries by brute force over all N rows (one warp per query), in the same
+// fp32 order as the rescoring; for the queries the candidate lists may have cut short, and for
+// small sets.  qlist == nullptr: queries 0..nq-1.
+__global__ void knn_brute(const float *__restrict__ base, int64_t N, int d, const float *__restrict__ queries,
+                          const int32_t *__restrict__ qlist, int nq, int k, int64_t self_base,
+                          int32_t *__restrict__ out_ids) {
+    extern __shared__ unsigned char sm[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    float *td = reinterpret_cast<float *>(sm) + (size_t)wib * (k + 1);
+    int32_t *ti = reinterpret_cast<int32_t *>(reinterpret_cast<float *>(sm) + (size_t)wpb * (k + 1)) +
+                  (size_t)wib * (k + 1);
+    const bool vec4 =
+        (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(base) | reinterpret_cast<uintptr_t>(queries)) & 15) == 0;
+    for (int w = blockIdx.x * wpb + wib; w < nq; w += gridDim.x * wpb) {
+        const int qi = qlist ? qlist[w] : w;
+        const float *q = queries + (size_t)qi * d;
+        int n = 0;
+        for (int64_t r0 = 0; r0 < N; r0 += 32) {
+            const int64_t r = r0 + lane;
+            const bool ok = r < N && !(self_base >= 0 && r == self_base + qi);
+            const float dist = ok ? l2_chain(base + (size_t)r * d, q, d, vec4) : 0.0f;
+            const bool lt_last = n < k || dist < td[k - 1] || (dist == td[k - 1] && (int32_t)r < ti[k - 1]);
+            unsigned m = __ballot_sync(0xffffffffu, ok && lt_last);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const float dv = __shfl_sync(0xffffffffu, dist, src);
+                top_insert(td, ti, n, k, dv, (int32_t)(r0 + src), lane);
+            }
+        }
+        for (int j = lane; j < k; j += 32) out_ids[(size_t)qi * k + j] = j < n ? ti[j] : -1;
+        __syncwarp();
     }
 }
 
@@ -507,12 +598,13 @@ namespace gsx {
 
 // Top k of every query over the base set by (distance, id) from the tensor-core candidate lists.
 // The base is split into at least min_chunks chunks, and each 64-column half of a chunk keeps its
-// kCand best candidates, so the result is exact unless more than kCand of a query's k + 1 nearest
-// rows fall into one half-chunk (k <= kCand is always exact).  self_base >= 0 leaves base row
+// kCand best candidates: exact when k <= kCand.  With fp32_l2 (the graph build's distance) larger
+// k are exact too: queries for which a full list may have dropped a row of the top k are redone by
+// brute force (*rechecked, may be null, counts them).  self_base >= 0 leaves base row
 // self_base + qi out of query qi's list (kNN graph of the base set).
 int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k, int32_t ip,
                int min_chunks, int64_t self_base, int fp32_l2, int32_t *d_ids, float *d_dis, int32_t *exact_inputs,
-               cudaStream_t st) {
+               int32_t *rechecked, cudaStream_t st) {
     if (!d_base || !d_queries || !d_ids || N <= 0 || nq <= 0 || d <= 0) return fail(GSX_ERR_INVALID, "bad arguments");
     if (k <= 0 || k > 4 * kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", 4 * kCand);
     if (d > 128) return fail(GSX_ERR_UNSUPPORTED, "exact kNN supports d <= 128");
@@ -570,16 +662,36 @@ int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries
     knn_tc_kernel<<<std::min(units, nsm), kThreads, kSmemBytes, st>>>(mqh, mql, mxh, mxl, P);
     GSX_CUDA(cudaGetLastError());
     const int wpb = 4;
-    const size_t rs_smem = (size_t)wpb * ncand * 20;
+    // one spare double per warp past the candidates (the k-th distance for the recheck)
+    const size_t rs_smem = (size_t)wpb * (ncand + 1) * 20;
     if (rs_smem > 227 * 1024) return fail(GSX_ERR_UNSUPPORTED, "too many candidate lists");
+    DevBuf rlist;
+    int32_t *recheck = nullptr;
+    if (fp32_l2) {
+        if ((rc = rlist.ensure((size_t)(nq + 1) * 4))) return rc;
+        GSX_CUDA(cudaMemsetAsync(rlist.p, 0, 4, st));
+        recheck = rlist.as<int32_t>();
+    }
     GSX_CUDA(cudaFuncSetAttribute(rescore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem));
-    rescore<<<(nq + wpb - 1) / wpb, wpb * 32, rs_smem, st>>>(d_base, d_queries, nq, d, (int)ncand, P.cand, P.ip, k,
-                                                             d_ids, d_dis, self_base, fp32_l2);
+    rescore<<<(nq + wpb - 1) / wpb, wpb * 32, rs_smem, st>>>(d_base, d_queries, nq, d, (int)ncand, P.cand,
+                                                             P.cand_d, P.ip, k, d_ids, d_dis, self_base, fp32_l2,
+                                                             recheck);
     GSX_CUDA(cudaGetLastError());
     unsigned err = 0;
     GSX_CUDA(cudaMemcpyAsync(&err, cnt.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
+    int32_t n_re = 0;
+    if (recheck) GSX_CUDA(cudaMemcpyAsync(&n_re, recheck, 4, cudaMemcpyDeviceToHost, st));
     GSX_CUDA(cudaStreamSynchronize(st));
     if (err) return fail(GSX_ERR_TIMEOUT, "tensor-core kNN kernel gave up waiting on a pipeline barrier");
+    if (n_re > 0) {
+        const int bw = 4;
+        const size_t bs = (size_t)bw * (k + 1) * 8;
+        knn_brute<<<std::min((n_re + bw - 1) / bw, 16 * nsm), bw * 32, bs, st>>>(d_base, N, d, d_queries, recheck + 1,
+                                                                                n_re, k, self_base, d_ids);
+        GSX_CUDA(cudaGetLastError());
+        GSX_CUDA(cudaStreamSynchronize(st));
+    }
+    if (rechecked) *rechecked = n_re;
     return GSX_OK;
 }
 
@@ -589,5 +701,6 @@ extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const fl
                              int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream) {
     if (!d_dis) return fail(GSX_ERR_INVALID, "bad arguments");
     if (k > kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", kCand);
-    return knn_select(d_base, N, d, d_queries, nq, k, ip, 1, -1, 0, d_ids, d_dis, exact_inputs, (cudaStream_t)stream);
+    return knn_select(d_base, N, d, d_queries, nq, k, ip, 1, -1, 0, d_ids, d_dis, exact_inputs, nullptr,
+                      (cudaStream_t)stream);
 }

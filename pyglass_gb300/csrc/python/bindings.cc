@@ -271,7 +271,7 @@ struct Searcher {
 struct Index {
     std::string type;
     int R = 32, L = 0;
-    double secs[6] = {0, 0, 0, 0, 0, 0};
+    double secs[7] = {0, 0, 0, 0, 0, 0, 0};
     py::object knng = py::none();
 
     Index(const std::string &index_type, const std::string &metric, const std::string &quant, int R_, int L_)
@@ -318,6 +318,7 @@ struct Index {
         d["connect_s"] = secs[3];
         d["total_s"] = secs[4];
         d["attached"] = (int64_t)secs[5];
+        d["knn_rows_rechecked"] = (int64_t)secs[6];
         return d;
     }
 };

@@ -62,6 +62,38 @@ def test_integer_data_matches_oracle(glass, oracle, tmp_path, kind, n, d, R, L):
     assert idx.stages()["attached"] == watt
 
 
+@pytest.mark.parametrize("n", [2, 3, 65, 150])
+def test_small_sets_match_oracle(glass, oracle, tmp_path, n):
+    """Fewer rows than candidate slots: every row's kNN list comes from the brute-force pass."""
+    from oracle import pyoracle
+
+    x = np.random.default_rng(n).integers(0, 16, size=(n, 16)).astype(np.float32)
+    g, idx = _build(glass, x, "NSG", 8, 0)
+    adj, ep = _adj(glass, g, tmp_path)
+    want, wep, wkn, watt = pyoracle.nsg_build(x, 8, 0, False)
+    np.testing.assert_array_equal(idx.knn_graph, wkn)
+    assert ep == wep
+    np.testing.assert_array_equal(adj, want)
+
+
+def test_rows_sorted_by_cluster_match_oracle(glass, oracle, tmp_path):
+    """Rows stored cluster by cluster put a row's nearest neighbours into one 64-column half of the
+    tensor-core tiles, more than its 16-entry candidate list holds: those rows must be found and
+    redone by brute force."""
+    from oracle import pyoracle
+
+    rng = np.random.default_rng(4)
+    centers = rng.integers(0, 200, size=(30, 24))
+    x = np.concatenate([np.clip(c + rng.integers(-3, 4, size=(100, 24)), 0, 255) for c in centers]).astype(np.float32)
+    g, idx = _build(glass, x, "SSG", 16, 0)
+    assert idx.stages()["knn_rows_rechecked"] > 0
+    adj, ep = _adj(glass, g, tmp_path)
+    want, wep, wkn, watt = pyoracle.nsg_build(x, 16, 0, True)
+    np.testing.assert_array_equal(idx.knn_graph, wkn)
+    assert ep == wep
+    np.testing.assert_array_equal(adj, want)
+
+
 @pytest.mark.parametrize("kind", ["NSG", "SSG"])
 def test_float_data_matches_oracle(glass, oracle, tmp_path, kind):
     from oracle import pyoracle
