@@ -3,7 +3,9 @@
 Workload (synthetic stand-in, seeded; the reference's ann-benchmarks sets are not available):
 1,000,000 x 128 base vectors from 1,024 Gaussian clusters (integers 0..255), 10,000 queries from
 the same mixture, NSG graph R=32 L=50 built by the reference's CPU builder (data/clusters1m.glass,
-made by oracle/build_graphs.py), searcher SQ4U + FP32 refine, k=10.
+made by oracle/build_graphs.py), searcher SQ4U + FP32 refine, k=10.  On a host without that file
+both arms search the NSG R=32 L=50 graph that this package's GPU builder makes (deterministic;
+the JSON line's config.graph says which graph was searched).
 
 A step is one batched search of all 10,000 queries at the headline ef.  `value` is QPS with the
 queries resident in HBM (CUDA events on the launching stream, L2 flushed by a 512 MB write
@@ -51,13 +53,43 @@ def args_():
     return p.parse_args()
 
 
+_BUILT = {}
+
+
 def graph_file():
+    """(path, format) of the searched graph: the reference-built file under data/, else (on a host
+    without it) the same NSG R=32 L=50 built by this package's GPU builder with FP32 distances,
+    saved once per process to a temporary glass file.  The GPU build is deterministic, so every
+    process that falls back searches the same graph."""
     from pyglass_gb300 import datasets
 
     found = datasets.graph_file(WORKLOAD, ROOT)
-    if found is None:
-        raise SystemExit(json.dumps({"error": f"data/{WORKLOAD}.glass missing: run python oracle/build_graphs.py {WORKLOAD}"}))
-    return found
+    if found is not None:
+        return found
+    if "path" not in _BUILT:
+        import tempfile
+
+        from pyglass_gb300 import glass
+
+        if glass.device_count() == 0:
+            raise SystemExit(json.dumps({"error": f"data/{WORKLOAD}.glass missing and no GPU to build it: "
+                                                  f"run python oracle/build_graphs.py {WORKLOAD}"}))
+        base = datasets.WORKLOADS[WORKLOAD]["base"]()
+        t = time.perf_counter()
+        g = glass.Index("NSG", "L2", "FP32", 32, 50).build(base)
+        _BUILT["seconds"] = time.perf_counter() - t
+        path = os.path.join(tempfile.mkdtemp(), f"{WORKLOAD}_gpu_built.glass")
+        g.save(path)
+        _BUILT["path"] = path
+    return _BUILT["path"], "glass"
+
+
+def graph_source():
+    """How the searched graph was made, for the JSON line."""
+    if "path" in _BUILT:
+        return (f"NSG R=32 L=50 built by this package's GPU builder (FP32 distances, {_BUILT['seconds']:.1f} s): "
+                "the reference-built graph file was absent on this host")
+    return "NSG R=32 L=50 built by the reference's CPU builder (build quant SQ8U)"
 
 
 def glass_path():
@@ -77,19 +109,19 @@ def glass_path():
 def load_workload():
     from pyglass_gb300 import datasets
 
-    graph_file()
-    meta = json.load(open(META))
     w = datasets.WORKLOADS[WORKLOAD]
     base, queries = w["base"](), w["queries"]()
-    if datasets.checksum(base) != meta["base_checksum"]:
+    meta = json.load(open(META)) if os.path.exists(META) else {}
+    if meta and datasets.checksum(base) != meta["base_checksum"]:
         raise SystemExit(json.dumps({"error": "synthetic base differs from the one the graph was built on"}))
     return base, queries, meta
 
 
 def workload_config(ef, nq, extra=None):
-    c = {"workload": "1,000,000 x 128 from 1,024 clusters (sigma 12, integers 0..255); NSG R=32 L=50 built by "
-                     "the reference CPU builder; 10,000 queries; SQ4U + FP32 refine (reorder 15); k=10",
-         "nq": nq, "k": K, "ef": ef, "metric": "L2", "quantizer": "SQ4U", "refine_quant": "FP32"}
+    c = {"workload": "1,000,000 x 128 from 1,024 clusters (sigma 12, integers 0..255); NSG R=32 L=50; "
+                     "10,000 queries; SQ4U + FP32 refine (reorder 15); k=10",
+         "graph": graph_source(), "nq": nq, "k": K, "ef": ef, "metric": "L2", "quantizer": "SQ4U",
+         "refine_quant": "FP32"}
     if extra:
         c.update(extra)
     return c
@@ -243,7 +275,7 @@ def graph_build_leg(glass, base, queries, gt, meta, ef, ref_recall):
     s2.set_ef(ef)
     ids, _ = s2.batch_search(queries, K)
     out = {"index": "NSG R=32 L=50, FP32 distances, exact 64-NN graph", "seconds": wall, "stages": idx.stages(),
-           "recall@10_at_ef": {"ef": ef, "gpu_built": recall(ids, gt), "reference_built": ref_recall},
+           "recall@10_at_ef": {"ef": ef, "gpu_built": recall(ids, gt), "searched_graph": ref_recall},
            "reference_cpu_seconds": meta.get("build_seconds"),
            "reference_cpu_note": "the reference's NSG builder (NN-Descent, SQ8U distances) on 8 x86 cores"}
     del s2, g
@@ -383,6 +415,10 @@ def run_gpu(a):
         print(json.dumps({"profile": True, "ef": a.ef, "step_ms": step_ms, "tuning": tuning}))
         return
     value, total_s = replica_throughput(sum(step_ms) / 1000.0, nq, a.steps, world, dist, "cuda")
+    # kernels of this package per step: the search launch, plus the two batch-order kernels
+    # (order_keys, order_sort) unless the tuning turned the ordering off (prefetch bit 4); 10,000
+    # queries exceed the resident warps of one launch, which is when the ordering runs
+    launches_per_step = 1 + (0 if tuning["prefetch"] & 16 else 2)
     ms_per_step = 1000.0 * total_s / a.steps
 
     # algorithmic bytes of one launch: per query n_dist*csize + n_expand*4K + reorder_k rows of
@@ -457,7 +493,7 @@ def run_gpu(a):
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "avg_dist_cmps": float(c.mean()),
                          "avg_expansions": float(x.mean())},
-            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": a.steps, "clocks": clk.summary(),
+            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": a.steps * launches_per_step, "clocks": clk.summary(),
             "plain_per_query": plain, "batched_over_plain": value / world / plain["qps"], "sweep": sweep,
             "ground_truth": gt_info, "serving": serving, "graph_build": build,
         }

@@ -1,7 +1,7 @@
 """Builds the benchmark graphs with the reference's own CPU builders (oracle/_ref).
 
 Graph construction is not part of the GPU path: the reference's HNSW/NSG builders write the
-glass graph file (glass/graph.hpp:106-119) that both the GPU searcher and the CPU checkers read.
+glass graph file (glass/graph.hpp:106-119) that both the GPU searcher and the CPU oracle read.
 Output: data/<workload>.glass plus data/<workload>.json (data checksums, build time).  Run here,
 where the reference checkout exists; the files travel with the repository snapshot.
 

@@ -1,7 +1,7 @@
 /*
  * glass_oracle.h - CPU restatement of the pyglass graph-search path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker the parity suite compares the GPU path against,
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the parity suite compares the GPU path against,
  * and the CPU baseline that bench.py times on the host cores.  The product (pyglass_gb300) never
  * links, loads or calls it.
  *

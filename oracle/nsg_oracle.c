@@ -1,5 +1,5 @@
 /* TEST INFRASTRUCTURE ONLY: a CPU restatement of the NSG / SSG graph build, used by the tests as
- * the checker of the GPU build (pyglass_gb300/csrc/build_kernel.cu); never part of the product.
+ * the oracle of the GPU build (pyglass_gb300/csrc/build_kernel.cu); never part of the product.
  *
  * It follows the reference's builder glass/nsg/nsg.hpp stage by stage:
  *   - kNN graph: exact by brute force ((distance, id) order over the fp32 distance below, the row

@@ -1,4 +1,4 @@
-"""ctypes access to the two CPU checkers (TEST INFRASTRUCTURE ONLY).
+"""ctypes access to the two CPU oracle libraries (TEST INFRASTRUCTURE ONLY).
 
 * ``Oracle`` wraps ``_build/libglass_oracle.so``: our C restatement of the reference search path
   (``oracle/glass_oracle.c``).  It runs everywhere gcc does, including the GPU host.
