@@ -112,6 +112,29 @@ int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, in
  * (synchronises the searcher's stream). */
 int gsx_searcher_overflow_count(gsx_searcher *s, uint32_t *count);
 
+/* ---- CUDA-graph form of the device batch (no reference counterpart) ----------------------- */
+typedef struct gsx_batch_graph gsx_batch_graph;
+
+/* Captures gsx_searcher_search_batch_device with these arguments (the searcher's current ef and
+ * tuning) as one CUDA graph: work-queue reset, batch-order kernels and the persistent search.
+ * Replays (gsx_batch_graph_launch) read the same device buffers, so a caller refills d_queries
+ * (and d_ef / d_k) in place between launches.  The call synchronises the device, runs the batch
+ * once without capture (the outputs then hold its results), and returns the graph.  The graph owns
+ * its scratch (queue counters, status words, order keys, visited tables); it uses the searcher's
+ * resident index, so it must be destroyed before the searcher and is invalid after a new
+ * gsx_searcher_set_data.  As in the device batch, a query whose visited table overflows is left
+ * as -1/inf and counted (gsx_batch_graph_overflow_count). */
+int gsx_searcher_capture_batch(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
+                               const int32_t *d_ef, const int32_t *d_k, int32_t kmax, int32_t *d_ids, float *d_dis,
+                               int32_t *d_cmps, int32_t *d_expansions, gsx_batch_graph **out);
+/* One replay on `stream` (cudaStream_t, NULL = the searcher's stream), without a host
+ * synchronisation.  Replays of one graph run one after another, whichever streams they go to. */
+int gsx_batch_graph_launch(gsx_batch_graph *g, void *stream);
+/* Queries of the latest replay left unanswered (waits for that replay). */
+int gsx_batch_graph_overflow_count(gsx_batch_graph *g, uint32_t *count);
+/* Waits for the latest replay and frees the graph and its scratch; NULL is accepted. */
+int gsx_batch_graph_destroy(gsx_batch_graph *g);
+
 /* Allocation-free batched search; no counterpart in the reference.  For callers that may not
  * allocate device memory while they serve: engines that hand all GPU memory to their own pool at
  * start-up, and latency-bound paths that cannot take the device-wide synchronisation an allocation

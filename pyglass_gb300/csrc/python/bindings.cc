@@ -73,6 +73,46 @@ Graph *graph_from_adjacency(i32arr adj, i32arr eps) {
     return G;
 }
 
+// A captured device batch (gsx_searcher_capture_batch); the Python object keeps its searcher alive.
+struct BatchGraph {
+    gsx_batch_graph *g = nullptr;
+    explicit BatchGraph(gsx_batch_graph *h) : g(h) {}
+    ~BatchGraph() { close(); }
+    BatchGraph(const BatchGraph &) = delete;
+    BatchGraph &operator=(const BatchGraph &) = delete;
+    gsx_batch_graph *live() const {
+        if (!g) throw std::runtime_error("glass-gb300: the batch graph is closed");
+        return g;
+    }
+    void launch(uintptr_t stream) {
+        gsx_batch_graph *h = live();
+        int rc;
+        {
+            py::gil_scoped_release l;
+            rc = gsx_batch_graph_launch(h, (void *)stream);
+        }
+        check(rc);
+    }
+    unsigned overflow_count() {
+        gsx_batch_graph *h = live();
+        uint32_t c = 0;
+        int rc;
+        {
+            py::gil_scoped_release l;
+            rc = gsx_batch_graph_overflow_count(h, &c);
+        }
+        check(rc);
+        return c;
+    }
+    void close() {
+        if (g) {
+            py::gil_scoped_release l;
+            gsx_batch_graph_destroy(g);
+        }
+        g = nullptr;
+    }
+};
+
 struct Searcher {
     gsx_searcher *s = nullptr;
     int32_t dim = 0;
@@ -181,6 +221,20 @@ struct Searcher {
         uint32_t c = 0;
         check(gsx_searcher_overflow_count(s, &c));
         return c;
+    }
+
+    BatchGraph *capture_batch_device(uintptr_t queries, int nq, int k, uintptr_t ids, uintptr_t dis, uintptr_t ef_per,
+                                     uintptr_t k_per, int kmax, uintptr_t cmps, uintptr_t expansions) {
+        gsx_batch_graph *h = nullptr;
+        int rc;
+        {
+            py::gil_scoped_release l;
+            rc = gsx_searcher_capture_batch(s, (const float *)queries, nq, k, (const int32_t *)ef_per,
+                                            (const int32_t *)k_per, kmax, (int32_t *)ids, (float *)dis,
+                                            (int32_t *)cmps, (int32_t *)expansions, &h);
+        }
+        check(rc);
+        return new BatchGraph(h);
     }
 
     py::array_t<double> distances(py::object query, py::object ids, bool refine) {
@@ -462,6 +516,10 @@ PYBIND11_MODULE(_glass, m) {
              py::arg("ids"), py::arg("dis"), py::arg("ef_per") = 0, py::arg("k_per") = 0, py::arg("kmax") = 0,
              py::arg("cmps") = 0, py::arg("expansions") = 0, py::arg("stream") = 0)
         .def("overflow_count", &Searcher::overflow_count)
+        .def("capture_batch_device", &Searcher::capture_batch_device, py::arg("queries"), py::arg("nq"), py::arg("k"),
+             py::arg("ids"), py::arg("dis"), py::arg("ef_per") = 0, py::arg("k_per") = 0, py::arg("kmax") = 0,
+             py::arg("cmps") = 0, py::arg("expansions") = 0, py::return_value_policy::take_ownership,
+             py::keep_alive<0, 1>())
         .def("optimize", &Searcher::optimize, py::arg("num_threads") = 0)
         .def("get_last_search_dist_cmps", &Searcher::get_last_search_avg_dist_cmps)
         .def("distances", &Searcher::distances, py::arg("query"), py::arg("ids"), py::arg("refine") = false)
@@ -471,6 +529,11 @@ PYBIND11_MODULE(_glass, m) {
         .def("set_tuning", &Searcher::set_tuning, py::arg("warps_per_block") = 0, py::arg("table_bits") = 0,
              py::arg("lanes_per_row") = 0, py::arg("prefetch") = 2, py::arg("spill_bits") = 0)
         .def("memory", &Searcher::memory);
+
+    py::class_<BatchGraph>(m, "BatchGraph")
+        .def("launch", &BatchGraph::launch, py::arg("stream") = 0)
+        .def("overflow_count", &BatchGraph::overflow_count)
+        .def("close", &BatchGraph::close);
 
     py::class_<Index>(m, "Index")
         .def(py::init<const std::string &, const std::string &, const std::string &, int, int>(), py::arg("index_type"),

@@ -8,6 +8,7 @@ extension is missing: there is no CPU fallback.
 
 try:
     from pyglass_gb300._glass import (  # noqa: F401
+        BatchGraph,
         Graph,
         Index,
         Searcher,
@@ -24,5 +25,5 @@ except ImportError as e:  # pragma: no cover - exercised only on a broken instal
         f"(nvcc for sm_103a is required): {e}"
     ) from e
 
-__all__ = ["Graph", "Index", "Searcher", "Server", "build_graph", "knn_exact", "set_num_threads", "device_count",
+__all__ = ["BatchGraph", "Graph", "Index", "Searcher", "Server", "build_graph", "knn_exact", "set_num_threads", "device_count",
            "version"]
