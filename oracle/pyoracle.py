@@ -251,6 +251,11 @@ def _ref_lib():
         lib.ref_searcher_dist_cmps.argtypes = [C.c_void_p]
         lib.ref_searcher_dist_cmps.restype = C.c_double
         lib.ref_searcher_destroy.argtypes = [C.c_void_p]
+        lib.ref_graph_open.argtypes = [C.c_char_p, C.c_char_p]
+        lib.ref_graph_open.restype = C.c_void_p
+        lib.ref_graph_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        lib.ref_graph_copy.argtypes = [C.c_void_p, _i32p, _i32p]
+        lib.ref_graph_close.argtypes = [C.c_void_p]
         lib.ref_code_size.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
         lib.ref_encode.argtypes = [C.c_char_p, C.c_char_p, _f32p, C.c_int, C.c_int, _u8p, _f32p]
         lib.ref_query_distances.argtypes = [C.c_char_p, C.c_char_p, _f32p, C.c_int, C.c_int, _f32p, C.c_int, _i32p,
@@ -271,6 +276,19 @@ class RefGlass:
         data = np.ascontiguousarray(data, dtype=np.float32)
         return _ref_lib().ref_build_graph(index_type.encode(), data, data.shape[0], data.shape[1], metric.encode(),
                                           quant.encode(), int(R), int(L), path.encode())
+
+    @staticmethod
+    def load_graph(path, fmt="glass"):
+        """(entry points, N x K adjacency) of a graph file as the reference's loader reads it."""
+        lib = _ref_lib()
+        h = lib.ref_graph_open(path.encode(), fmt.encode())
+        n, k, nep = C.c_int(), C.c_int(), C.c_int()
+        lib.ref_graph_info(h, C.byref(n), C.byref(k), C.byref(nep))
+        eps = np.zeros(nep.value, np.int32)
+        adj = np.zeros((n.value, k.value), np.int32)
+        lib.ref_graph_copy(h, eps, adj)
+        lib.ref_graph_close(h)
+        return eps, adj
 
     @staticmethod
     def encode(quant, metric, data):

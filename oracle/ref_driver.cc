@@ -10,7 +10,7 @@
 //   GraphSearcherBase::SetData/Search/SearchBatch/SetEf/GetLastSearchAvgDistCmps
 //                                      glass/searcher/searcher_base.hpp:7-19
 //   glass::create_hnsw / create_nsg    glass/hnsw/hnsw.hpp:74-133, glass/nsg/nsg.hpp:411-434
-//   Graph<int>::load/save             glass/graph.hpp:106-153
+//   Graph<int>::load/save             glass/graph.hpp:106-153 (load in every format, :121-245)
 //   Quantizer train/add/get_computer   glass/quant/*.hpp
 #include <omp.h>
 
@@ -136,6 +136,29 @@ void ref_searcher_search_batch(void *h, const float *qs, int nq, int k, int *ids
 double ref_searcher_dist_cmps(void *h) { return ((RefSearcher *)h)->s->GetLastSearchAvgDistCmps(); }
 
 void ref_searcher_destroy(void *h) { delete (RefSearcher *)h; }
+
+// A graph read by the reference's own loader (Graph<int>::load, glass/graph.hpp:121-135, with its
+// glass / diskann / hnswlib / nsg readers), for comparison with the product's loaders.
+void *ref_graph_open(const char *path, const char *format) {
+    auto *g = new glass::Graph<int>;
+    g->load(path, format);
+    return g;
+}
+
+void ref_graph_info(void *h, int *N, int *K, int *nep) {
+    auto *g = (glass::Graph<int> *)h;
+    *N = g->N;
+    *K = g->K;
+    *nep = (int)g->eps.size();
+}
+
+void ref_graph_copy(void *h, int *eps, int *adj) {
+    auto *g = (glass::Graph<int> *)h;
+    std::memcpy(eps, g->eps.data(), g->eps.size() * 4);
+    std::memcpy(adj, g->data, (size_t)g->N * g->K * 4);
+}
+
+void ref_graph_close(void *h) { delete (glass::Graph<int> *)h; }
 
 // Code size in bytes of one encoded row for quantizer `quant` at dimension d.
 int ref_code_size(const char *quant, const char *metric, int d) {

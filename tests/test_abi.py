@@ -108,6 +108,53 @@ def test_nsg_and_diskann_formats(lib, tmp_path):
     np.testing.assert_array_equal(_adj(lib, h2, 4, 3), want)
 
 
+def _write_hnswlib(path, rows, maxM0, ep, max_level=0, d=4):
+    """An hnswlib index file as the reference's loader reads it (glass/graph.hpp:184-217): header
+    fields it skips are written as zeros; each level-0 element is a 32-bit link count, maxM0
+    links, the vector and its 8-byte label."""
+    size_per = 4 * (maxM0 + 1) + 4 * d + 8
+    with open(path, "wb") as f:
+        np.array([0, len(rows), len(rows), size_per, 0, 0], np.uint64).tofile(f)
+        np.array([max_level, ep], np.int32).tofile(f)
+        np.array([maxM0, maxM0], np.uint64).tofile(f)  # maxM, maxM0
+        f.write(bytes(24))  # M, mult, ef_construction
+        for i, r in enumerate(rows):
+            links = np.full(maxM0, 123456, np.int32)  # unused slots hold junk; only the count matters
+            links[: len(r)] = r
+            np.array([len(r)], np.int32).tofile(f)
+            links.tofile(f)
+            np.full(d, 0.5, np.float32).tofile(f)
+            np.array([i], np.uint64).tofile(f)
+
+
+def test_hnswlib_level0_format(lib, tmp_path):
+    rng = np.random.default_rng(3)
+    N, maxM0 = 40, 6
+    rows = [list(rng.choice(N, size=int(rng.integers(0, maxM0 + 1)), replace=False).astype(int)) for _ in range(N)]
+    p = str(tmp_path / "g.hnswlib")
+    _write_hnswlib(p, rows, maxM0, ep=7)
+    rc, h = _load(lib, p, "hnswlib")
+    assert rc == 0
+    assert _info(lib, h)[:3] == [N, maxM0, 1]
+    want = np.full((N, maxM0), -1, np.int32)
+    for i, r in enumerate(rows):
+        want[i, : len(r)] = r
+    np.testing.assert_array_equal(_adj(lib, h, N, maxM0), want)
+    # a file with upper levels: the reference stops with "Not supported"; here it is an error code
+    p2 = str(tmp_path / "multi.hnswlib")
+    _write_hnswlib(p2, rows, maxM0, ep=7, max_level=2)
+    rc, _ = _load(lib, p2, "hnswlib")
+    assert rc == 7  # GSX_ERR_UNSUPPORTED
+    # a count larger than the row holds is rejected instead of read past the row
+    p3 = str(tmp_path / "bad.hnswlib")
+    _write_hnswlib(p3, [[1, 2]] + rows[1:], maxM0, ep=0)
+    with open(p3, "r+b") as f:
+        f.seek(96)  # first element's link count
+        np.array([maxM0 + 1], np.int32).tofile(f)
+    rc, _ = _load(lib, p3, "hnswlib")
+    assert rc == 1
+
+
 def test_malformed_graphs_are_rejected(lib, tmp_path):
     p = str(tmp_path / "bad.glass")
     write_glass(p, np.array([[1, 5], [0, -1]], np.int32), [0])  # id 5 >= N

@@ -66,3 +66,51 @@ def test_search_nsg_clusters(oracle, ref, tmp_path):
             np.testing.assert_array_equal(ri, oi)
             np.testing.assert_array_equal(rdis, odis)
             assert rs.get_last_search_dist_cmps() == os_.get_last_search_dist_cmps()
+
+
+@pytest.mark.parametrize("fmt", ["glass", "nsg", "diskann", "hnswlib"])
+def test_graph_loaders_match_the_reference(ref, glass, tmp_path, fmt):
+    """Each graph format read by the library's loader (gsx_graph_load) gives the entry points and
+    the -1 padded adjacency that the reference's Graph<int>::load gives for the same file."""
+    import ctypes as C
+
+    from tests.helpers import write_glass
+    from tests.test_abi import _adj, _info, _load, _write_hnswlib
+
+    rng = np.random.default_rng(17)
+    N, K = 300, 12
+    rows = [list(rng.choice(N, size=int(rng.integers(0, K + 1)), replace=False).astype(int)) for _ in range(N)]
+    rows[5] = list(rng.choice(N, size=K, replace=False).astype(int))  # a full row
+    ep = 42
+    p = str(tmp_path / f"g.{fmt}")
+    if fmt == "glass":
+        adj = np.full((N, K), -1, np.int32)
+        for i, r in enumerate(rows):
+            adj[i, : len(r)] = r
+        write_glass(p, adj, [ep, 7])
+    elif fmt in ("nsg", "diskann"):
+        body = b"".join(np.array([len(r)] + r, np.int32).tobytes() for r in rows)
+        with open(p, "wb") as f:
+            if fmt == "nsg":  # glass/graph.hpp:219-245
+                np.array([K, ep], np.int32).tofile(f)
+            else:  # glass/graph.hpp:155-182
+                np.array([24 + len(body)], np.uint64).tofile(f)
+                np.array([K, ep], np.int32).tofile(f)
+                np.array([0], np.uint64).tofile(f)
+            f.write(body)
+    else:
+        _write_hnswlib(p, rows, K, ep)
+    want_eps, want_adj = ref.load_graph(p, fmt)
+    lib = C.CDLL(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "pyglass_gb300",
+                              "libglass_gb300.so"))
+    rc, h = _load(lib, p, fmt)
+    assert rc == 0
+    n, k, nep, _ = _info(lib, h)
+    assert (n, k) == want_adj.shape and nep == want_eps.size
+    np.testing.assert_array_equal(_adj(lib, h, n, k), want_adj)
+    got_eps = np.zeros(nep, np.int32)
+    lib.gsx_graph_eps.argtypes = [C.c_void_p, C.c_void_p]
+    assert lib.gsx_graph_eps(h, got_eps.ctypes.data) == 0
+    np.testing.assert_array_equal(got_eps, want_eps)
+    lib.gsx_graph_destroy.argtypes = [C.c_void_p]
+    lib.gsx_graph_destroy(h)
