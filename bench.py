@@ -129,7 +129,11 @@ def workload_config(ef, nq, extra=None):
 
 def cpu_baseline(base, queries, ef, sample):
     """The oracle (C restatement of the reference searcher, OpenMP over all host cores) on a
-    bounded sample of the workload."""
+    bounded sample of the workload, timed the way the reference's example harness times
+    batch_search (examples/main.py:166-187: one warm-up, best of 5), plus its plain form (`search`,
+    one query per call, one thread) on a few hundred queries."""
+    import platform
+
     from oracle import pyoracle
 
     pyoracle.build(ref=False)
@@ -137,15 +141,22 @@ def cpu_baseline(base, queries, ef, sample):
     s = pyoracle.Searcher(g, base, "L2", "SQ4U", "FP32")
     s.set_ef(ef)
     q = queries[:sample]
-    s.batch_search(q[:200], K)  # warm-up
+    s.batch_search(q, K)  # warm-up
     best = 1e30
-    for _ in range(3):
+    for _ in range(5):
         t = time.perf_counter()
         s.batch_search(q, K)
         best = min(best, time.perf_counter() - t)
+    n_plain = min(200, sample)
+    t = time.perf_counter()
+    for i in range(n_plain):
+        s.search(q[i], K)
+    plain_qps = n_plain / (time.perf_counter() - t)
     cores = os.cpu_count() or 1
-    return {"value": sample / best, "unit": "QPS", "cores": cores, "kind": "port",
-            "sample": f"{sample} of the 10,000 queries at ef={ef}, best of 3, {cores} OpenMP threads"}, s
+    return {"value": sample / best, "unit": "QPS", "cores": cores, "kind": "port", "host": platform.machine(),
+            "sample": f"{sample} of the 10,000 queries at ef={ef}, one warm-up then best of 5, {cores} OpenMP threads",
+            "plain_single_thread_qps": plain_qps,
+            "plain_sample": f"search() on the first {n_plain} queries, one per call, one thread"}, s
 
 
 class Clocks:
