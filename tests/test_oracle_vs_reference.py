@@ -114,3 +114,55 @@ def test_graph_loaders_match_the_reference(ref, glass, tmp_path, fmt):
     np.testing.assert_array_equal(got_eps, want_eps)
     lib.gsx_graph_destroy.argtypes = [C.c_void_p]
     lib.gsx_graph_destroy(h)
+
+
+def _workload_graph(name):
+    """(glass path, base, queries) of a benchmark workload whose reference-built graph is present
+    under data/ (made by oracle/build_graphs.py), else skip."""
+    import json
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = os.path.join(root, "data", f"{name}.glass")
+    meta = os.path.join(root, "data", f"{name}.json")
+    if not (os.path.exists(path) and os.path.exists(meta)):
+        pytest.skip(f"data/{name}.glass not present (built by oracle/build_graphs.py)")
+    w = datasets.WORKLOADS[name]
+    base = w["base"]()
+    if datasets.checksum(base) != json.load(open(meta))["base_checksum"]:
+        pytest.skip(f"{name}: base rows differ from the ones the graph was built on")
+    return path, base, w["queries"]()
+
+
+@pytest.mark.parametrize("name, cases", [
+    # 960-d low-rank rows, HNSW R=32 L=200 (upper levels exercised): E5M2 and SQ8U, L2
+    ("lowrank100k", [("E5M2", "", "L2"), ("SQ8U", "", "L2")]),
+    # 768-d unit vectors, NSG R=48 L=100, inner product: SQ4U first pass with FP32 rerank, and FP16
+    ("sphere200k", [("SQ4U", "FP32", "IP"), ("FP16", "", "IP")]),
+    # 1M x 128 clusters, NSG R=32 L=50: the benchmark searcher
+    ("clusters1m", [("SQ4U", "FP32", "L2")]),
+])
+def test_search_on_workload_graphs(oracle, ref, name, cases):
+    """The oracle's searches equal the compiled reference's (ids, distances, distance counts) on the
+    reference-built graphs of the workload shapes, at several ef and k in {10, 100}."""
+    path, base, queries = _workload_graph(name)
+    q = queries[:64]
+    g = oracle.Graph(path)
+    for quant, refine, metric in cases:
+        rs = ref.Searcher(path, base, metric, quant, refine)
+        os_ = oracle.Searcher(g, base, metric, quant, refine)
+        for ef, k in [(64, 10), (128, 100)]:
+            rs.set_ef(ef)
+            os_.set_ef(ef)
+            ri, rdis = rs.batch_search(q, k)
+            oi, odis = os_.batch_search(q, k)
+            np.testing.assert_array_equal(ri, oi, err_msg=f"{quant}/{refine}/{metric} ef={ef} k={k}")
+            np.testing.assert_array_equal(rdis, odis, err_msg=f"{quant}/{refine}/{metric} ef={ef} k={k}")
+            assert rs.get_last_search_dist_cmps() == os_.get_last_search_dist_cmps()
+        # the single-query form (expansion limit max(k, ef)) on a few queries
+        rs.set_ef(32)
+        os_.set_ef(32)
+        for i in range(4):
+            a, b = rs.search(q[i], 10), os_.search(q[i], 10)
+            np.testing.assert_array_equal(a[0], b[0])
+            np.testing.assert_array_equal(a[1], b[1])
+        del rs, os_
