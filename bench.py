@@ -293,6 +293,32 @@ def graph_build_leg(glass, base, queries, gt, meta, ef, ref_recall):
     return out
 
 
+def graph_replay_leg(torch, s, dq, nq, steps, stream, flush, want_ids):
+    """The headline batch captured once as a CUDA graph (Searcher.capture_batch_device) and
+    replayed `steps` times on the bench stream: QPS from CUDA events (L2 flushed between replays)
+    and whether the ids equal those of the direct launches."""
+    try:
+        ids = torch.empty((nq, K), dtype=torch.int32, device="cuda")
+        dis = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        g = s.capture_batch_device(dq.data_ptr(), nq, K, ids.data_ptr(), dis.data_ptr(), kmax=K)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            g.launch(stream.cuda_stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in ev)
+        out = {"qps": nq / (ms / 1000.0), "ms_per_replay": ms, "replays": steps,
+               "overflowed_queries": g.overflow_count(),
+               "same_ids_as_direct_launches": bool(np.array_equal(ids.cpu().numpy(), want_ids))}
+        g.close()
+        return out
+    except Exception as e:  # reported, not fatal: the headline numbers above stand on their own
+        return {"error": str(e)[:300]}
+
+
 def replica_throughput(local_seconds, nq, steps, world, dist=None, device="cpu"):
     """Whole-job QPS of `world` replicas that each searched nq queries per step: the slowest
     rank's time bounds the job (max over ranks; no data is exchanged)."""
@@ -490,6 +516,7 @@ def run_gpu(a):
 
     serving = serving_leg(glass, s, queries)
     build = graph_build_leg(glass, base, queries, gt, meta, a.ef, rec) if rank == 0 else None
+    replay = graph_replay_leg(torch, s, dq, nq, max(3, a.steps // 4), stream, flush, out_ids)
 
     if rank == 0:
         cb, _ = cpu_baseline(base, queries, a.ef, min(a.cpu_sample, nq))
@@ -506,7 +533,7 @@ def run_gpu(a):
                          "avg_expansions": float(x.mean())},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": a.steps * launches_per_step, "clocks": clk.summary(),
             "plain_per_query": plain, "batched_over_plain": value / world / plain["qps"], "sweep": sweep,
-            "ground_truth": gt_info, "serving": serving, "graph_build": build,
+            "ground_truth": gt_info, "serving": serving, "graph_build": build, "cuda_graph_replay": replay,
         }
         print(json.dumps(line))
     if dist:
