@@ -342,9 +342,10 @@ double go_distance(int kind, int metric, const void *qenc, const uint8_t *code, 
                                                          * c read as 8c+4 on the query's 0..127 scale */
         const uint8_t *x = (const uint8_t *)qenc, *y = code;
         int32_t s = 0;
-        for (int i = 0; i < dalign; ++i) {
-            int32_t c = (y[i / 2] >> ((i & 1) * 4)) & 15, t = (int32_t)x[i] - (8 * c + 4);
-            s += t * t;
+        for (int j = 0; j < dalign / 2; ++j) {   /* dims 2j (low nibble) and 2j+1 (high nibble) */
+            const int32_t t0 = (int32_t)x[2 * j] - (8 * (y[j] & 15) + 4);
+            const int32_t t1 = (int32_t)x[2 * j + 1] - (8 * (y[j] >> 4) + 4);
+            s += t0 * t0 + t1 * t1;
         }
         return (double)s;
     }
@@ -357,18 +358,20 @@ double go_distance(int kind, int metric, const void *qenc, const uint8_t *code, 
     if (kind == GO_SQ2U) {                            /* l2a_u2_u2 (x86/l2_impl.hpp:301-333): L2 on 2-bit codes, both metrics */
         const uint8_t *x = (const uint8_t *)qenc, *y = code;
         int32_t s = 0;
-        for (int i = 0; i < dalign; ++i) {
-            int32_t a = (x[i / 4] >> ((i & 3) * 2)) & 3, b = (y[i / 4] >> ((i & 3) * 2)) & 3;
-            s += (a - b) * (a - b);
+        for (int j = 0; j < dalign / 4; ++j) {   /* dims 4j+k at bits 2k of byte j */
+            const int32_t a = x[j], b = y[j];
+            const int32_t d0 = (a & 3) - (b & 3), d1 = ((a >> 2) & 3) - ((b >> 2) & 3);
+            const int32_t d2 = ((a >> 4) & 3) - ((b >> 4) & 3), d3 = (a >> 6) - (b >> 6);
+            s += d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
         }
         return (double)s;
     }
     if (kind == GO_SQ4U) {                            /* l2_u4_u4_ref (ref/l2_ref.hpp:67-77); L2 for both metrics */
         const uint8_t *x = (const uint8_t *)qenc, *y = code;
         int32_t s = 0;
-        for (int i = 0; i < dalign; ++i) {
-            int32_t a = (x[i / 2] >> ((i & 1) * 4)) & 15, b = (y[i / 2] >> ((i & 1) * 4)) & 15;
-            s += (a - b) * (a - b);
+        for (int j = 0; j < dalign / 2; ++j) {   /* dims 2j (low nibble) and 2j+1 (high nibble) */
+            const int32_t d0 = (x[j] & 15) - (y[j] & 15), d1 = (x[j] >> 4) - (y[j] >> 4);
+            s += d0 * d0 + d1 * d1;
         }
         return (double)s;
     }
@@ -570,6 +573,11 @@ static void initialize_search(const go_graph *g, pool_t *p, computer_t *c) {
 
 /* SearchImpl2 (graph_searcher.hpp:196-224); SearchImpl1 (:161-194) visits the same nodes in the
  * same order and inserts the same distances, so one loop serves both. */
+/* Prefetch distance for code rows: the reference's default `po` of 1 (graph_searcher.hpp:29), each
+ * row's cache lines in full.  Only timing depends on it. */
+#ifndef GO_PREFETCH_AHEAD
+#define GO_PREFETCH_AHEAD 1
+#endif
 static void search_impl(const go_graph *g, pool_t *p, computer_t *c, int32_t *edge) {
     while (pool_has_next(p)) {
         int32_t u = pool_pop(p);
@@ -582,7 +590,17 @@ static void search_impl(const go_graph *g, pool_t *p, computer_t *c, int32_t *ed
             vis_set(p, v);
             edge[n++] = v;
         }
-        for (int i = 0; i < n; ++i) pool_insert(p, edge[i], comp_dist(c, edge[i]));
+        /* prefetch the code rows of the next neighbours, as the reference does (:211-218) */
+        const int64_t cs = c->ix->csize;
+        const uint8_t *codes = c->ix->codes;
+        for (int i = 0; i < n && i < GO_PREFETCH_AHEAD; ++i)
+            for (int64_t b = 0; b < cs; b += 64) __builtin_prefetch(codes + (int64_t)edge[i] * cs + b, 0, 3);
+        for (int i = 0; i < n; ++i) {
+            if (i + GO_PREFETCH_AHEAD < n)
+                for (int64_t b = 0; b < cs; b += 64)
+                    __builtin_prefetch(codes + (int64_t)edge[i + GO_PREFETCH_AHEAD] * cs + b, 0, 3);
+            pool_insert(p, edge[i], comp_dist(c, edge[i]));
+        }
     }
 }
 
