@@ -156,8 +156,9 @@ def cpu_baseline(base, queries, ef, sample):
     return {"value": sample / best, "unit": "QPS", "cores": cores, "kind": "port", "host": platform.machine(),
             "sample": f"{sample} of the 10,000 queries at ef={ef}, one warm-up then best of 5, {cores} OpenMP threads",
             "plain_single_thread_qps": plain_qps,
-            "port_vs_reference": "on x86 (8 cores, same workload, ef=128) the port runs at about 0.75x the compiled "
-                                 "reference's batch QPS (47k vs 62-63k); the reference is not available on this host",
+            "port_vs_reference": "on x86 (8 cores, same workload, ef=128, interleaved runs) the port runs at "
+                                 "0.58-0.75x the compiled reference's batch QPS (37-47k vs 62-64k); the reference "
+                                 "is not available on this host",
             "plain_sample": f"search() on the first {n_plain} queries, one per call, one thread"}, s
 
 
