@@ -74,4 +74,4 @@ def test_null_arguments_give_error_codes(glass):
         if name in NO_HANDLE_OK:
             assert res[name] == 0, name
         else:
-            assert res[name] != 0, f"{name} accepted null arguments"
+            assert res[name] == 1, f"{name} returned {res[name]} for null arguments, not GSX_ERR_INVALID"
