@@ -7,6 +7,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <new>
 #include <numeric>
 #include <random>
 #include <string>
@@ -485,6 +487,28 @@ int server_resolve_one(gsx_searcher *s, const float *q, int k, int ef, int32_t *
     return rc;
 }
 
+// Attaches HNSW upper levels to a host graph (HNSWInitializer layout, glass/hnsw/HNSWInitializer.hpp:22-86).
+// Built on a copy and swapped in only when valid, so the graph is unchanged on any error.
+int set_levels(HostGraph &h, int32_t hK, int32_t ep, const int32_t *levels, const int32_t *lists) {
+    if (h.N == 0) return fail(GSX_ERR_STATE, "graph is empty");
+    HostGraph t = h;
+    t.has_hnsw = 1;
+    t.hK = hK;
+    t.hep = ep;
+    t.levels.assign(levels, levels + t.N);
+    t.loff.assign((size_t)t.N + 1, 0);
+    for (int32_t u = 0; u < t.N; ++u) {
+        if (t.levels[u] < 0) return fail(GSX_ERR_INVALID, "negative level for node %d", u);
+        t.loff[u + 1] = t.loff[u] + (int64_t)t.levels[u] * hK;
+    }
+    if (t.loff[t.N] > 0 && !lists) return fail(GSX_ERR_INVALID, "null level lists");
+    t.lists.assign(lists, lists + t.loff[t.N]);
+    const int rc = validate_graph(t);
+    if (rc) return rc;
+    h = std::move(t);
+    return GSX_OK;
+}
+
 }  // namespace gsx
 
 using namespace gsx;
@@ -506,57 +530,43 @@ int gsx_device_count(void) {
 
 int gsx_graph_load(const char *filename, const char *format, gsx_graph **out) {
     if (!filename || !out) return fail(GSX_ERR_INVALID, "null argument");
-    auto *g = new gsx_graph;
-    int rc = graph_load(filename, format, g->g);
-    if (rc) {
-        delete g;
-        return rc;
+    try {
+        std::unique_ptr<gsx_graph> g(new gsx_graph);
+        int rc = graph_load(filename, format, g->g);
+        if (rc) return rc;
+        *out = g.release();
+        return GSX_OK;
+    } catch (const std::bad_alloc &) {
+        return fail(GSX_ERR_NOMEM, "out of host memory loading '%s'", filename);
     }
-    *out = g;
-    return GSX_OK;
 }
 
 int gsx_graph_create(const int32_t *adj, int32_t N, int32_t K, const int32_t *eps, int32_t nep, gsx_graph **out) {
     if (!adj || !out || N <= 0 || K <= 0 || nep < 0 || (nep && !eps)) return fail(GSX_ERR_INVALID, "bad graph arguments");
-    auto *g = new gsx_graph;
-    g->g.N = N;
-    g->g.K = K;
-    g->g.adj.assign(adj, adj + (size_t)N * K);
-    g->g.eps.assign(eps, eps + nep);
-    int rc = validate_graph(g->g);
-    if (rc) {
-        delete g;
-        return rc;
+    if (K > kMaxDegree) return fail(GSX_ERR_UNSUPPORTED, "graph degree %d exceeds %d", K, kMaxDegree);
+    try {
+        std::unique_ptr<gsx_graph> g(new gsx_graph);
+        g->g.N = N;
+        g->g.K = K;
+        g->g.adj.assign(adj, adj + (size_t)N * K);
+        g->g.eps.assign(eps, eps + nep);
+        int rc = validate_graph(g->g);
+        if (rc) return rc;
+        *out = g.release();
+        return GSX_OK;
+    } catch (const std::bad_alloc &) {
+        return fail(GSX_ERR_NOMEM, "out of host memory for a %d x %d graph", N, K);
     }
-    *out = g;
-    return GSX_OK;
 }
 
 int gsx_graph_set_levels(gsx_graph *g, int32_t hK, int32_t ep, const int32_t *levels, const int32_t *lists) {
     if (!g || !levels || (hK <= 0)) return fail(GSX_ERR_INVALID, "bad level arguments");
-    HostGraph &h = g->g;
-    if (h.N == 0) return fail(GSX_ERR_STATE, "graph is empty");
-    HostGraph saved = h;
-    h.has_hnsw = 1;
-    h.hK = hK;
-    h.hep = ep;
-    h.levels.assign(levels, levels + h.N);
-    h.loff.assign((size_t)h.N + 1, 0);
-    for (int32_t u = 0; u < h.N; ++u) {
-        if (h.levels[u] < 0) {
-            h = saved;
-            return fail(GSX_ERR_INVALID, "negative level for node %d", u);
-        }
-        h.loff[u + 1] = h.loff[u] + (int64_t)h.levels[u] * hK;
+    if (hK > kMaxDegree) return fail(GSX_ERR_UNSUPPORTED, "HNSW level degree %d unsupported", hK);
+    try {
+        return set_levels(g->g, hK, ep, levels, lists);
+    } catch (const std::bad_alloc &) {
+        return fail(GSX_ERR_NOMEM, "out of host memory for the HNSW levels");
     }
-    if (h.loff[h.N] > 0 && !lists) {
-        h = saved;
-        return fail(GSX_ERR_INVALID, "null level lists");
-    }
-    h.lists.assign(lists, lists + h.loff[h.N]);
-    int rc = validate_graph(h);
-    if (rc) h = saved;
-    return rc;
 }
 
 int gsx_graph_save(const gsx_graph *g, const char *filename) {

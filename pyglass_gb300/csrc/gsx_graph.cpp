@@ -17,30 +17,51 @@ bool rd(std::ifstream &f, T *p, size_t n = 1) {
     return (bool)f;
 }
 
+// Bytes from the read position to the end of the file.  Every size a header claims is checked
+// against it before anything is allocated for it, so a malformed file is an error, never a huge
+// allocation.
+uint64_t bytes_left(std::ifstream &f) {
+    const std::streamoff at = f.tellg();
+    f.seekg(0, std::ios::end);
+    const std::streamoff end = f.tellg();
+    f.seekg(at);
+    return (at >= 0 && end >= at) ? (uint64_t)(end - at) : 0;
+}
+
+int degree_unsupported(int32_t K) { return fail(GSX_ERR_UNSUPPORTED, "graph degree %d exceeds %d", K, kMaxDegree); }
+
 int load_glass(const char *path, HostGraph &g) {
     std::ifstream f(path, std::ios::binary);
     if (!f) return fail(GSX_ERR_IO, "cannot open graph file '%s'", path);
+    uint64_t left = bytes_left(f);
     int32_t nep = 0;
-    if (!rd(f, &nep) || nep < 0 || nep > (1 << 24)) return fail(GSX_ERR_INVALID, "bad entry-point count in '%s'", path);
+    if (!rd(f, &nep) || nep < 0 || (uint64_t)nep * 4 > left - 4)
+        return fail(GSX_ERR_INVALID, "bad entry-point count in '%s'", path);
     g.eps.resize((size_t)nep);
     if (nep && !rd(f, g.eps.data(), (size_t)nep)) return fail(GSX_ERR_INVALID, "truncated graph file '%s'", path);
     if (!rd(f, &g.N) || !rd(f, &g.K) || g.N <= 0 || g.K <= 0)
         return fail(GSX_ERR_INVALID, "bad graph header in '%s'", path);
+    if (g.K > kMaxDegree) return degree_unsupported(g.K);
+    left = bytes_left(f);
+    if ((uint64_t)g.N * (uint64_t)g.K * 4 > left) return fail(GSX_ERR_INVALID, "truncated adjacency in '%s'", path);
     g.adj.resize((size_t)g.N * (size_t)g.K);
     if (!rd(f, g.adj.data(), g.adj.size())) return fail(GSX_ERR_INVALID, "truncated adjacency in '%s'", path);
+    left -= (uint64_t)g.adj.size() * 4;
     // optional HNSW upper levels (graph.hpp:282-285, HNSWInitializer.hpp:64-75)
     int32_t hn = 0;
     if (rd(f, &hn)) {
-        if (!rd(f, &g.hK) || !rd(f, &g.hep) || hn != g.N || g.hK <= 0)
+        if (!rd(f, &g.hK) || !rd(f, &g.hep) || hn != g.N || g.hK <= 0 || left < 12)
             return fail(GSX_ERR_INVALID, "bad HNSW level header in '%s'", path);
+        left -= 12;
         g.has_hnsw = 1;
         g.levels.assign((size_t)g.N, 0);
         g.loff.assign((size_t)g.N + 1, 0);
         g.lists.clear();
         for (int32_t i = 0; i < g.N; ++i) {
             int32_t cur = 0;
-            if (!rd(f, &cur) || cur < 0 || cur % g.hK != 0)
+            if (!rd(f, &cur) || cur < 0 || cur % g.hK != 0 || left < 4 || (uint64_t)cur * 4 > left - 4)
                 return fail(GSX_ERR_INVALID, "bad HNSW list of node %d in '%s'", i, path);
+            left -= 4 + (uint64_t)cur * 4;
             g.levels[i] = cur / g.hK;
             g.loff[i] = (int64_t)g.lists.size();
             size_t at = g.lists.size();
@@ -61,6 +82,7 @@ int load_nsg(const char *path, HostGraph &g) {
     f.seekg(0);
     int32_t ep = 0;
     if (!rd(f, &g.K) || !rd(f, &ep) || g.K <= 0) return fail(GSX_ERR_INVALID, "bad NSG header in '%s'", path);
+    if (g.K > kMaxDegree) return degree_unsupported(g.K);
     g.eps.assign(1, ep);
     std::vector<int32_t> buf;
     std::vector<std::vector<int32_t>> rows;
@@ -85,6 +107,7 @@ int load_diskann(const char *path, HostGraph &g) {
     int32_t ep = 0;
     if (!rd(f, &size) || !rd(f, &g.K) || !rd(f, &ep) || !rd(f, &frozen) || g.K <= 0)
         return fail(GSX_ERR_INVALID, "bad DiskANN header in '%s'", path);
+    if (g.K > kMaxDegree) return degree_unsupported(g.K);
     g.eps.assign(1, ep);
     std::vector<std::vector<int32_t>> rows;
     std::vector<int32_t> buf;
@@ -118,8 +141,10 @@ int load_hnswlib(const char *path, HostGraph &g) {
     f.seekg(8, std::ios::cur);
     rd(f, &maxM0);
     f.seekg(24, std::ios::cur);
-    if (!f || max_el == 0 || max_el > (1u << 31) || maxM0 == 0 || size_per < 4 * (maxM0 + 1))
+    if (!f || max_el == 0 || max_el > (1u << 31) - 1 || maxM0 == 0 || size_per < 4 * (maxM0 + 1))
         return fail(GSX_ERR_INVALID, "bad hnswlib header in '%s'", path);
+    if (maxM0 > (uint64_t)kMaxDegree) return degree_unsupported(maxM0 > (1u << 30) ? (1 << 30) : (int32_t)maxM0);
+    if (size_per > bytes_left(f) / max_el) return fail(GSX_ERR_INVALID, "truncated hnswlib file '%s'", path);
     g.N = (int32_t)max_el;
     g.K = (int32_t)maxM0;
     g.eps.assign(1, ep);

@@ -209,3 +209,54 @@ def test_compact_nsg_twin_roundtrip(glass, tmp_path):
     again = str(tmp_path / "again.glass")
     glass.Graph(twin, "nsg").save(again)
     assert open(again, "rb").read() == open(src, "rb").read()
+
+
+_HOSTILE = r"""
+import ctypes as C, sys
+lib = C.CDLL(sys.argv[1])
+lib.gsx_graph_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]
+lib.gsx_graph_create.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]
+h = C.c_void_p()
+for path, fmt in zip(sys.argv[2::2], sys.argv[3::2]):
+    print(path.rsplit("/", 1)[-1], lib.gsx_graph_load(path.encode(), fmt.encode(), C.byref(h)), flush=True)
+one = (C.c_int32 * 1)(0)
+print("create", lib.gsx_graph_create(one, 1 << 30, 1 << 30, one, 1, C.byref(h)), flush=True)
+"""
+
+
+def test_hostile_headers_are_errors_not_allocations(lib, tmp_path):
+    """Header fields that claim more rows, wider rows or longer lists than the file holds are
+    rejected before anything is allocated for them (a malformed file must not exhaust host memory
+    or end the process)."""
+    import subprocess
+    import sys
+
+    files = []
+
+    def add(name, fmt, *arrays):
+        p = str(tmp_path / name)
+        with open(p, "wb") as f:
+            for a in arrays:
+                a.tofile(f)
+        files.extend([p, fmt])
+
+    i32, u64 = np.int32, np.uint64
+    add("huge_n.glass", "glass", np.array([1, 0, 1 << 30, 48], i32))               # 200 GB of rows, 16-byte file
+    add("huge_nk.glass", "glass", np.array([1, 0, 1 << 30, 1 << 30], i32))         # N*K overflows 32 bits
+    add("wide.nsg", "nsg", np.array([1 << 30, 0, 1, 0], i32))                      # K = 2^30
+    add("wide.diskann", "diskann", np.array([40], u64), np.array([1 << 30, 0], i32), np.array([0], u64),
+        np.array([1, 0], i32))
+    add("huge.hnswlib", "hnswlib", np.array([0, (1 << 31) - 1, 0, 1 << 40, 0, 0], u64), np.array([0, 0], i32),
+        np.array([32, 32], u64), np.zeros(24, np.uint8))
+    adj = np.array([[1], [0]], i32)
+    add("huge_levels.glass", "glass", np.array([1, 0, 2, 1], i32), adj.ravel(), np.array([2, 1, 0], i32),
+        np.array([1 << 30], i32))                                                  # one node claims 2^30 list entries
+    lib_path = os.path.join(ROOT, "pyglass_gb300", "libglass_gb300.so")
+    r = subprocess.run([sys.executable, "-c", _HOSTILE, lib_path, *files], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, f"crashed: {r.stdout[-500:]} {r.stderr[-1500:]}"
+    got = dict(line.split() for line in r.stdout.splitlines())
+    for name in ("huge_n.glass", "huge.hnswlib", "huge_levels.glass"):
+        assert got[name] == "1", (name, got[name])      # GSX_ERR_INVALID: the file does not hold what it claims
+    for name in ("huge_nk.glass", "wide.nsg", "wide.diskann"):
+        assert got[name] == "7", (name, got[name])      # GSX_ERR_UNSUPPORTED: degree above 64
+    assert got["create"] == "7"
