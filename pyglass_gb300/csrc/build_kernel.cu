@@ -761,187 +761,189 @@ using namespace gsx;
 
 extern "C" int gsx_graph_build_nsg(const float *data, int64_t N, int32_t d, int32_t R, int32_t L, int32_t use_ssg,
                                    int32_t knn_k, int32_t *knng_out, double *seconds, gsx_graph **out) {
-    if (!data || !out || N < 2 || d <= 0 || R <= 0 || L < 0 || knn_k <= 0)
-        return fail(GSX_ERR_INVALID, "bad graph-build arguments");
-    if (N > (int64_t)INT32_MAX) return fail(GSX_ERR_INVALID, "N too large");
-    if (R > 256 || knn_k > 64) return fail(GSX_ERR_UNSUPPORTED, "R <= 256 and knn_k <= 64 are supported");
-    if (d > 128) return fail(GSX_ERR_UNSUPPORTED, "the GPU graph build supports d <= 128 (tensor-core kNN)");
-    if (L == 0) L = R + 32;  // nsg.hpp:47
-    const int C = R + 100;
-    const int K = (int)std::min<int64_t>(knn_k, N - 1);
-    int dev = 0, nsm = 0, ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-        cudaGetLastError();
-        return fail(GSX_ERR_CUDA, "no CUDA device is visible");
-    }
-    GSX_CUDA(cudaGetDevice(&dev));
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaStream_t st = nullptr;
-    GSX_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct StreamGuard {
-        cudaStream_t s;
-        ~StreamGuard() {
-            cudaStreamSynchronize(s);
-            cudaStreamDestroy(s);
+    try {
+        if (!data || !out || N < 2 || d <= 0 || R <= 0 || L < 0 || knn_k <= 0)
+            return fail(GSX_ERR_INVALID, "bad graph-build arguments");
+        if (N > (int64_t)INT32_MAX) return fail(GSX_ERR_INVALID, "N too large");
+        if (R > 256 || knn_k > 64) return fail(GSX_ERR_UNSUPPORTED, "R <= 256 and knn_k <= 64 are supported");
+        if (d > 128) return fail(GSX_ERR_UNSUPPORTED, "the GPU graph build supports d <= 128 (tensor-core kNN)");
+        if (L == 0) L = R + 32;  // nsg.hpp:47
+        const int C = R + 100;
+        const int K = (int)std::min<int64_t>(knn_k, N - 1);
+        int dev = 0, nsm = 0, ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            return fail(GSX_ERR_CUDA, "no CUDA device is visible");
         }
-    } guard{st};
-    double t[5] = {0, 0, 0, 0, 0};
-    const double t0 = now_s();
-    int rc;
-    DevBuf x, knng, cen, sums, best, ids, dis, visb, cnt, ovl, indeg, off, tot, fillc, src, sd, fin;
-    if ((rc = x.ensure((size_t)N * d * 4)) || (rc = knng.ensure((size_t)N * K * 4))) return rc;
-    GSX_CUDA(cudaMemcpyAsync(x.p, data, (size_t)N * d * 4, cudaMemcpyHostToDevice, st));
-    // 1. kNN graph, in query blocks that keep the candidate lists near 1 GB
-    const int64_t qblock = 1 << 18;
-    int64_t n_re = 0;
-    for (int64_t q0 = 0; q0 < N; q0 += qblock) {
-        const int nq = (int)std::min<int64_t>(qblock, N - q0);
-        int32_t re = 0;
-        if ((rc = knn_select(x.as<float>(), N, d, x.as<float>() + q0 * d, nq, K, 0, 16, q0, 1,
-                             knng.as<int32_t>() + q0 * K, nullptr, nullptr, &re, st)))
-            return rc;
-        n_re += re;
-    }
-    // 2. entry point
-    if ((rc = sums.ensure((size_t)d * 8)) || (rc = cen.ensure((size_t)d * 4)) || (rc = best.ensure(8))) return rc;
-    GSX_CUDA(cudaMemsetAsync(sums.p, 0, (size_t)d * 8, st));
-    GSX_CUDA(cudaMemsetAsync(best.p, 0xff, 8, st));
-    column_sums<<<dim3((d + 31) / 32, 2 * nsm), 256, 0, st>>>(x.as<float>(), N, d, sums.as<double>());
-    centroid_of<<<1, 256, 0, st>>>(sums.as<double>(), N, d, cen.as<float>());
-    nearest_to<<<4 * nsm, 256, 0, st>>>(x.as<float>(), N, d, cen.as<float>(), best.as<unsigned long long>());
-    GSX_CUDA(cudaGetLastError());
-    unsigned long long bk = 0;
-    GSX_CUDA(cudaMemcpyAsync(&bk, best.p, 8, cudaMemcpyDeviceToHost, st));
-    GSX_CUDA(cudaStreamSynchronize(st));
-    const int32_t ep = (int32_t)(unsigned)bk;
-    if (knng_out) GSX_CUDA(cudaMemcpy(knng_out, knng.p, (size_t)N * K * 4, cudaMemcpyDeviceToHost));
-    const double t1 = now_s();
-    t[0] = t1 - t0;
-    // 3. link
-    LinkParams P{};
-    P.x = x.as<float>();
-    P.N = (int)N;
-    P.d = d;
-    P.vec4 = (d % 4) == 0;
-    P.knng = knng.as<int32_t>();
-    P.K = K;
-    P.ep = ep;
-    P.L = L;
-    P.C = C;
-    P.R = R;
-    P.ssg = use_ssg ? 1 : 0;
-    P.threshold = (float)std::cos(60.0 / 180.0 * 3.14159265358979323846264);  // nsg.hpp:40
-    if ((rc = ids.ensure((size_t)N * R * 4)) || (rc = dis.ensure((size_t)N * R * 4)) || (rc = cnt.ensure(16)) ||
-        (rc = ovl.ensure((size_t)N * 4)))
-        return rc;
-    P.out_ids = ids.as<int32_t>();
-    P.out_dis = dis.as<float>();
-    P.counter = cnt.as<unsigned>();
-    P.n_overflow = cnt.as<unsigned>() + 1;
-    P.overflow_nodes = ovl.as<int32_t>();
-    const size_t per_warp = (size_t)(L + 1) * 8 + (size_t)(C + 1) * 8 + (size_t)R * 8 + (size_t)K * 8;
-    const size_t link_smem = per_warp * kLinkWarps;
-    if (link_smem > 200 * 1024) return fail(GSX_ERR_UNSUPPORTED, "L or R too large for the link kernel");
-    GSX_CUDA(cudaFuncSetAttribute(nsg_link, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)link_smem));
-    int per_sm = 0;
-    GSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nsg_link, 32 * kLinkWarps, link_smem));
-    per_sm = std::max(1, per_sm);
-    // pass 1: 2^14-slot visited tables; nodes whose search outgrows them run again with 2^20 slots
-    // on fewer warps
-    std::vector<int32_t> redo;
-    for (int pass = 0; pass < 2; ++pass) {
-        const int bits = pass == 0 ? 14 : 20;
-        int blocks = pass == 0 ? per_sm * nsm : std::min(per_sm * nsm, std::max(1, (int)((redo.size() + 7) / 8)));
-        if (pass == 1) {
-            if (redo.empty()) break;
-            blocks = std::min(blocks, 32);
+        GSX_CUDA(cudaGetDevice(&dev));
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaStream_t st = nullptr;
+        GSX_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
+        } guard{st};
+        double t[5] = {0, 0, 0, 0, 0};
+        const double t0 = now_s();
+        int rc;
+        DevBuf x, knng, cen, sums, best, ids, dis, visb, cnt, ovl, indeg, off, tot, fillc, src, sd, fin;
+        if ((rc = x.ensure((size_t)N * d * 4)) || (rc = knng.ensure((size_t)N * K * 4))) return rc;
+        GSX_CUDA(cudaMemcpyAsync(x.p, data, (size_t)N * d * 4, cudaMemcpyHostToDevice, st));
+        // 1. kNN graph, in query blocks that keep the candidate lists near 1 GB
+        const int64_t qblock = 1 << 18;
+        int64_t n_re = 0;
+        for (int64_t q0 = 0; q0 < N; q0 += qblock) {
+            const int nq = (int)std::min<int64_t>(qblock, N - q0);
+            int32_t re = 0;
+            if ((rc = knn_select(x.as<float>(), N, d, x.as<float>() + q0 * d, nq, K, 0, 16, q0, 1,
+                                 knng.as<int32_t>() + q0 * K, nullptr, nullptr, &re, st)))
+                return rc;
+            n_re += re;
         }
-        if ((rc = visb.ensure(((size_t)blocks * kLinkWarps) << bits << 3))) return rc;
-        GSX_CUDA(cudaMemsetAsync(visb.p, 0, ((size_t)blocks * kLinkWarps) << bits << 3, st));
-        GSX_CUDA(cudaMemsetAsync(cnt.p, 0, 8, st));
-        P.vis = visb.as<unsigned long long>();
-        P.vis_bits = bits;
-        DevBuf nodes;
-        if (pass == 0) {
-            P.nodes = nullptr;
-            P.n_nodes = (int)N;
-        } else {
-            if ((rc = nodes.ensure(redo.size() * 4))) return rc;
-            GSX_CUDA(cudaMemcpyAsync(nodes.p, redo.data(), redo.size() * 4, cudaMemcpyHostToDevice, st));
-            P.nodes = nodes.as<int32_t>();
-            P.n_nodes = (int)redo.size();
-        }
-        nsg_link<<<blocks, 32 * kLinkWarps, link_smem, st>>>(P);
+        // 2. entry point
+        if ((rc = sums.ensure((size_t)d * 8)) || (rc = cen.ensure((size_t)d * 4)) || (rc = best.ensure(8))) return rc;
+        GSX_CUDA(cudaMemsetAsync(sums.p, 0, (size_t)d * 8, st));
+        GSX_CUDA(cudaMemsetAsync(best.p, 0xff, 8, st));
+        column_sums<<<dim3((d + 31) / 32, 2 * nsm), 256, 0, st>>>(x.as<float>(), N, d, sums.as<double>());
+        centroid_of<<<1, 256, 0, st>>>(sums.as<double>(), N, d, cen.as<float>());
+        nearest_to<<<4 * nsm, 256, 0, st>>>(x.as<float>(), N, d, cen.as<float>(), best.as<unsigned long long>());
         GSX_CUDA(cudaGetLastError());
-        unsigned hc[2] = {0, 0};
-        GSX_CUDA(cudaMemcpyAsync(hc, cnt.p, 8, cudaMemcpyDeviceToHost, st));
+        unsigned long long bk = 0;
+        GSX_CUDA(cudaMemcpyAsync(&bk, best.p, 8, cudaMemcpyDeviceToHost, st));
         GSX_CUDA(cudaStreamSynchronize(st));
-        redo.assign(hc[1], 0);
-        if (hc[1]) GSX_CUDA(cudaMemcpy(redo.data(), ovl.p, (size_t)hc[1] * 4, cudaMemcpyDeviceToHost));
-        if (pass == 1 && !redo.empty())
-            return fail(GSX_ERR_NOMEM, "%zu nodes visited more than 786,432 rows while linking", redo.size());
-    }
-    visb.release();
-    const double t2 = now_s();
-    t[1] = t2 - t1;
-    // 4. reverse links
-    const int64_t n_edges = N * (int64_t)R;
-    const int64_t nb = (N + 1023) / 1024;
-    if ((rc = indeg.ensure((size_t)N * 4)) || (rc = off.ensure((size_t)(N + 1) * 8)) ||
-        (rc = tot.ensure((size_t)(nb + 1) * 8)) || (rc = fillc.ensure((size_t)N * 4)) ||
-        (rc = src.ensure((size_t)n_edges * 4)) || (rc = sd.ensure((size_t)n_edges * 4)) ||
-        (rc = fin.ensure((size_t)n_edges * 4)))
-        return rc;
-    GSX_CUDA(cudaMemsetAsync(indeg.p, 0, (size_t)N * 4, st));
-    GSX_CUDA(cudaMemsetAsync(fillc.p, 0, (size_t)N * 4, st));
-    count_in<<<4 * nsm, 256, 0, st>>>(ids.as<int32_t>(), n_edges, indeg.as<unsigned>());
-    scan_blocks<<<(unsigned)nb, 1024, 0, st>>>(indeg.as<unsigned>(), N, off.as<int64_t>(), tot.as<int64_t>());
-    scan_totals<<<1, 1024, 0, st>>>(tot.as<int64_t>(), nb);
-    add_totals<<<(unsigned)nb, 1024, 0, st>>>(off.as<int64_t>(), N, tot.as<int64_t>());
-    fill_in<<<4 * nsm, 256, 0, st>>>(ids.as<int32_t>(), dis.as<float>(), n_edges, R, off.as<int64_t>(),
-                                      fillc.as<unsigned>(), src.as<int32_t>(), sd.as<float>());
-    GSX_CUDA(cudaGetLastError());
-    RevParams Q{};
-    Q.x = x.as<float>();
-    Q.N = (int)N;
-    Q.d = d;
-    Q.vec4 = P.vec4;
-    Q.R = R;
-    Q.ids = ids.as<int32_t>();
-    Q.dis = dis.as<float>();
-    Q.off = off.as<int64_t>();
-    Q.src = src.as<int32_t>();
-    Q.sd = sd.as<float>();
-    Q.out = fin.as<int32_t>();
-    const size_t rev_smem = (size_t)kRevWarps * 4 * R * 4;
-    GSX_CUDA(cudaFuncSetAttribute(reverse_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rev_smem));
-    reverse_merge<<<8 * nsm, 32 * kRevWarps, rev_smem, st>>>(Q);
-    GSX_CUDA(cudaGetLastError());
-    std::vector<int32_t> g((size_t)n_edges);
-    GSX_CUDA(cudaMemcpyAsync(g.data(), fin.p, (size_t)n_edges * 4, cudaMemcpyDeviceToHost, st));
-    GSX_CUDA(cudaStreamSynchronize(st));
-    const double t3 = now_s();
-    t[2] = t3 - t2;
-    // 5. connectivity
-    int32_t n_att = 0;
-    if ((rc = tree_grow(data, N, d, R, L, ep, g, &n_att))) return rc;
-    const double t4 = now_s();
-    t[3] = t4 - t3;
-    t[4] = t4 - t0;
-    auto *gr = new gsx_graph;
-    gr->g.N = (int32_t)N;
-    gr->g.K = R;
-    gr->g.adj.swap(g);
-    gr->g.eps.assign(1, ep);
-    if ((rc = validate_graph(gr->g))) {
-        delete gr;
-        return rc;
-    }
-    if (seconds) {
-        for (int i = 0; i < 5; ++i) seconds[i] = t[i];
-        seconds[5] = (double)n_att;
-        seconds[6] = (double)n_re;
-    }
-    *out = gr;
-    return GSX_OK;
+        const int32_t ep = (int32_t)(unsigned)bk;
+        if (knng_out) GSX_CUDA(cudaMemcpy(knng_out, knng.p, (size_t)N * K * 4, cudaMemcpyDeviceToHost));
+        const double t1 = now_s();
+        t[0] = t1 - t0;
+        // 3. link
+        LinkParams P{};
+        P.x = x.as<float>();
+        P.N = (int)N;
+        P.d = d;
+        P.vec4 = (d % 4) == 0;
+        P.knng = knng.as<int32_t>();
+        P.K = K;
+        P.ep = ep;
+        P.L = L;
+        P.C = C;
+        P.R = R;
+        P.ssg = use_ssg ? 1 : 0;
+        P.threshold = (float)std::cos(60.0 / 180.0 * 3.14159265358979323846264);  // nsg.hpp:40
+        if ((rc = ids.ensure((size_t)N * R * 4)) || (rc = dis.ensure((size_t)N * R * 4)) || (rc = cnt.ensure(16)) ||
+            (rc = ovl.ensure((size_t)N * 4)))
+            return rc;
+        P.out_ids = ids.as<int32_t>();
+        P.out_dis = dis.as<float>();
+        P.counter = cnt.as<unsigned>();
+        P.n_overflow = cnt.as<unsigned>() + 1;
+        P.overflow_nodes = ovl.as<int32_t>();
+        const size_t per_warp = (size_t)(L + 1) * 8 + (size_t)(C + 1) * 8 + (size_t)R * 8 + (size_t)K * 8;
+        const size_t link_smem = per_warp * kLinkWarps;
+        if (link_smem > 200 * 1024) return fail(GSX_ERR_UNSUPPORTED, "L or R too large for the link kernel");
+        GSX_CUDA(cudaFuncSetAttribute(nsg_link, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)link_smem));
+        int per_sm = 0;
+        GSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nsg_link, 32 * kLinkWarps, link_smem));
+        per_sm = std::max(1, per_sm);
+        // pass 1: 2^14-slot visited tables; nodes whose search outgrows them run again with 2^20 slots
+        // on fewer warps
+        std::vector<int32_t> redo;
+        for (int pass = 0; pass < 2; ++pass) {
+            const int bits = pass == 0 ? 14 : 20;
+            int blocks = pass == 0 ? per_sm * nsm : std::min(per_sm * nsm, std::max(1, (int)((redo.size() + 7) / 8)));
+            if (pass == 1) {
+                if (redo.empty()) break;
+                blocks = std::min(blocks, 32);
+            }
+            if ((rc = visb.ensure(((size_t)blocks * kLinkWarps) << bits << 3))) return rc;
+            GSX_CUDA(cudaMemsetAsync(visb.p, 0, ((size_t)blocks * kLinkWarps) << bits << 3, st));
+            GSX_CUDA(cudaMemsetAsync(cnt.p, 0, 8, st));
+            P.vis = visb.as<unsigned long long>();
+            P.vis_bits = bits;
+            DevBuf nodes;
+            if (pass == 0) {
+                P.nodes = nullptr;
+                P.n_nodes = (int)N;
+            } else {
+                if ((rc = nodes.ensure(redo.size() * 4))) return rc;
+                GSX_CUDA(cudaMemcpyAsync(nodes.p, redo.data(), redo.size() * 4, cudaMemcpyHostToDevice, st));
+                P.nodes = nodes.as<int32_t>();
+                P.n_nodes = (int)redo.size();
+            }
+            nsg_link<<<blocks, 32 * kLinkWarps, link_smem, st>>>(P);
+            GSX_CUDA(cudaGetLastError());
+            unsigned hc[2] = {0, 0};
+            GSX_CUDA(cudaMemcpyAsync(hc, cnt.p, 8, cudaMemcpyDeviceToHost, st));
+            GSX_CUDA(cudaStreamSynchronize(st));
+            redo.assign(hc[1], 0);
+            if (hc[1]) GSX_CUDA(cudaMemcpy(redo.data(), ovl.p, (size_t)hc[1] * 4, cudaMemcpyDeviceToHost));
+            if (pass == 1 && !redo.empty())
+                return fail(GSX_ERR_NOMEM, "%zu nodes visited more than 786,432 rows while linking", redo.size());
+        }
+        visb.release();
+        const double t2 = now_s();
+        t[1] = t2 - t1;
+        // 4. reverse links
+        const int64_t n_edges = N * (int64_t)R;
+        const int64_t nb = (N + 1023) / 1024;
+        if ((rc = indeg.ensure((size_t)N * 4)) || (rc = off.ensure((size_t)(N + 1) * 8)) ||
+            (rc = tot.ensure((size_t)(nb + 1) * 8)) || (rc = fillc.ensure((size_t)N * 4)) ||
+            (rc = src.ensure((size_t)n_edges * 4)) || (rc = sd.ensure((size_t)n_edges * 4)) ||
+            (rc = fin.ensure((size_t)n_edges * 4)))
+            return rc;
+        GSX_CUDA(cudaMemsetAsync(indeg.p, 0, (size_t)N * 4, st));
+        GSX_CUDA(cudaMemsetAsync(fillc.p, 0, (size_t)N * 4, st));
+        count_in<<<4 * nsm, 256, 0, st>>>(ids.as<int32_t>(), n_edges, indeg.as<unsigned>());
+        scan_blocks<<<(unsigned)nb, 1024, 0, st>>>(indeg.as<unsigned>(), N, off.as<int64_t>(), tot.as<int64_t>());
+        scan_totals<<<1, 1024, 0, st>>>(tot.as<int64_t>(), nb);
+        add_totals<<<(unsigned)nb, 1024, 0, st>>>(off.as<int64_t>(), N, tot.as<int64_t>());
+        fill_in<<<4 * nsm, 256, 0, st>>>(ids.as<int32_t>(), dis.as<float>(), n_edges, R, off.as<int64_t>(),
+                                          fillc.as<unsigned>(), src.as<int32_t>(), sd.as<float>());
+        GSX_CUDA(cudaGetLastError());
+        RevParams Q{};
+        Q.x = x.as<float>();
+        Q.N = (int)N;
+        Q.d = d;
+        Q.vec4 = P.vec4;
+        Q.R = R;
+        Q.ids = ids.as<int32_t>();
+        Q.dis = dis.as<float>();
+        Q.off = off.as<int64_t>();
+        Q.src = src.as<int32_t>();
+        Q.sd = sd.as<float>();
+        Q.out = fin.as<int32_t>();
+        const size_t rev_smem = (size_t)kRevWarps * 4 * R * 4;
+        GSX_CUDA(cudaFuncSetAttribute(reverse_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rev_smem));
+        reverse_merge<<<8 * nsm, 32 * kRevWarps, rev_smem, st>>>(Q);
+        GSX_CUDA(cudaGetLastError());
+        std::vector<int32_t> g((size_t)n_edges);
+        GSX_CUDA(cudaMemcpyAsync(g.data(), fin.p, (size_t)n_edges * 4, cudaMemcpyDeviceToHost, st));
+        GSX_CUDA(cudaStreamSynchronize(st));
+        const double t3 = now_s();
+        t[2] = t3 - t2;
+        // 5. connectivity
+        int32_t n_att = 0;
+        if ((rc = tree_grow(data, N, d, R, L, ep, g, &n_att))) return rc;
+        const double t4 = now_s();
+        t[3] = t4 - t3;
+        t[4] = t4 - t0;
+        auto *gr = new gsx_graph;
+        gr->g.N = (int32_t)N;
+        gr->g.K = R;
+        gr->g.adj.swap(g);
+        gr->g.eps.assign(1, ep);
+        if ((rc = validate_graph(gr->g))) {
+            delete gr;
+            return rc;
+        }
+        if (seconds) {
+            for (int i = 0; i < 5; ++i) seconds[i] = t[i];
+            seconds[5] = (double)n_att;
+            seconds[6] = (double)n_re;
+        }
+        *out = gr;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_graph_build_nsg")
 }

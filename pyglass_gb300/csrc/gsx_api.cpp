@@ -520,31 +520,31 @@ const char *gsx_last_error(void) { return g_err.c_str(); }
 const char *gsx_version(void) { return "glass-gb300 0.1.0 (sm_103a)"; }
 
 int gsx_device_count(void) {
-    int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    return n;
+    try {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return n;
+    } GSX_ABI_GUARD("gsx_device_count")
 }
 
 int gsx_graph_load(const char *filename, const char *format, gsx_graph **out) {
-    if (!filename || !out) return fail(GSX_ERR_INVALID, "null argument");
     try {
+        if (!filename || !out) return fail(GSX_ERR_INVALID, "null argument");
         std::unique_ptr<gsx_graph> g(new gsx_graph);
         int rc = graph_load(filename, format, g->g);
         if (rc) return rc;
         *out = g.release();
         return GSX_OK;
-    } catch (const std::bad_alloc &) {
-        return fail(GSX_ERR_NOMEM, "out of host memory loading '%s'", filename);
-    }
+    } GSX_ABI_GUARD("gsx_graph_load")
 }
 
 int gsx_graph_create(const int32_t *adj, int32_t N, int32_t K, const int32_t *eps, int32_t nep, gsx_graph **out) {
-    if (!adj || !out || N <= 0 || K <= 0 || nep < 0 || (nep && !eps)) return fail(GSX_ERR_INVALID, "bad graph arguments");
-    if (K > kMaxDegree) return fail(GSX_ERR_UNSUPPORTED, "graph degree %d exceeds %d", K, kMaxDegree);
     try {
+        if (!adj || !out || N <= 0 || K <= 0 || nep < 0 || (nep && !eps)) return fail(GSX_ERR_INVALID, "bad graph arguments");
+        if (K > kMaxDegree) return fail(GSX_ERR_UNSUPPORTED, "graph degree %d exceeds %d", K, kMaxDegree);
         std::unique_ptr<gsx_graph> g(new gsx_graph);
         g->g.N = N;
         g->g.K = K;
@@ -554,130 +554,136 @@ int gsx_graph_create(const int32_t *adj, int32_t N, int32_t K, const int32_t *ep
         if (rc) return rc;
         *out = g.release();
         return GSX_OK;
-    } catch (const std::bad_alloc &) {
-        return fail(GSX_ERR_NOMEM, "out of host memory for a %d x %d graph", N, K);
-    }
+    } GSX_ABI_GUARD("gsx_graph_create")
 }
 
 int gsx_graph_set_levels(gsx_graph *g, int32_t hK, int32_t ep, const int32_t *levels, const int32_t *lists) {
-    if (!g || !levels || (hK <= 0)) return fail(GSX_ERR_INVALID, "bad level arguments");
-    if (hK > kMaxDegree) return fail(GSX_ERR_UNSUPPORTED, "HNSW level degree %d unsupported", hK);
     try {
+        if (!g || !levels || (hK <= 0)) return fail(GSX_ERR_INVALID, "bad level arguments");
+        if (hK > kMaxDegree) return fail(GSX_ERR_UNSUPPORTED, "HNSW level degree %d unsupported", hK);
         return set_levels(g->g, hK, ep, levels, lists);
-    } catch (const std::bad_alloc &) {
-        return fail(GSX_ERR_NOMEM, "out of host memory for the HNSW levels");
-    }
+    } GSX_ABI_GUARD("gsx_graph_set_levels")
 }
 
 int gsx_graph_save(const gsx_graph *g, const char *filename) {
-    if (!g || !filename) return fail(GSX_ERR_INVALID, "null argument");
-    if (g->g.N == 0) return fail(GSX_ERR_STATE, "graph is empty (moved into a searcher?)");
-    return graph_save(g->g, filename);
+    try {
+        if (!g || !filename) return fail(GSX_ERR_INVALID, "null argument");
+        if (g->g.N == 0) return fail(GSX_ERR_STATE, "graph is empty (moved into a searcher?)");
+        return graph_save(g->g, filename);
+    } GSX_ABI_GUARD("gsx_graph_save")
 }
 
 int gsx_graph_info(const gsx_graph *g, int32_t *N, int32_t *K, int32_t *nep, int32_t *has_hnsw) {
-    if (!g) return fail(GSX_ERR_INVALID, "null graph");
-    if (N) *N = g->g.N;
-    if (K) *K = g->g.K;
-    if (nep) *nep = (int32_t)g->g.eps.size();
-    if (has_hnsw) *has_hnsw = g->g.has_hnsw;
-    return GSX_OK;
+    try {
+        if (!g) return fail(GSX_ERR_INVALID, "null graph");
+        if (N) *N = g->g.N;
+        if (K) *K = g->g.K;
+        if (nep) *nep = (int32_t)g->g.eps.size();
+        if (has_hnsw) *has_hnsw = g->g.has_hnsw;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_graph_info")
 }
 
 int gsx_graph_adjacency(const gsx_graph *g, int32_t *adj_out) {
-    if (!g || !adj_out) return fail(GSX_ERR_INVALID, "null argument");
-    std::memcpy(adj_out, g->g.adj.data(), g->g.adj.size() * 4);
-    return GSX_OK;
+    try {
+        if (!g || !adj_out) return fail(GSX_ERR_INVALID, "null argument");
+        std::memcpy(adj_out, g->g.adj.data(), g->g.adj.size() * 4);
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_graph_adjacency")
 }
 
 int gsx_graph_eps(const gsx_graph *g, int32_t *eps_out) {
-    if (!g || !eps_out) return fail(GSX_ERR_INVALID, "null argument");
-    std::memcpy(eps_out, g->g.eps.data(), g->g.eps.size() * 4);
-    return GSX_OK;
+    try {
+        if (!g || !eps_out) return fail(GSX_ERR_INVALID, "null argument");
+        std::memcpy(eps_out, g->g.eps.data(), g->g.eps.size() * 4);
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_graph_eps")
 }
 
 void gsx_graph_destroy(gsx_graph *g) { delete g; }
 
 int gsx_searcher_create(gsx_graph *graph, const char *metric, const char *quantizer, const char *refine_quant,
                         int device, gsx_searcher **out) {
-    if (!graph || !out) return fail(GSX_ERR_INVALID, "null argument");
-    if (graph->g.N == 0) return fail(GSX_ERR_STATE, "graph is empty (already moved into a searcher?)");
-    int ndev = gsx_device_count();
-    if (ndev == 0) return fail(GSX_ERR_CUDA, "no CUDA device is visible");
-    if (device < 0 || device >= ndev) return fail(GSX_ERR_INVALID, "device %d out of range", device);
-    int kind;
-    int rc = parse_quant(quantizer ? quantizer : "", &kind);
-    if (rc) return rc;
-    const std::string rq = refine_quant ? refine_quant : "";
-    // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ8/SQ4U, 3 for SQ2U, 1.0 otherwise (in which
-    // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
-    const float factor = (kind == K_SQ2U || kind == K_SQ1)                                           ? 3.0f
-                         : (kind == K_SQ8U || kind == K_SQ4U || kind == K_SQ8 || kind == K_SQ4UA) ? 1.5f
-                                                                                                  : 1.0f;
-    // make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer map
-    // does not know -> FP32 store; SQ8U / SQ8 -> their own refiners; any other known name -> none
-    int rkind = K_FP32;
-    bool refiner = false;
-    if (!rq.empty()) {
-        static const char *no_refiner[] = {"BF16", "E5M2", "SQ6", "SQ4U", "SQ4UA", "SQ4", "SQ8P", "SQ1", "SQ2U", "PQ8"};
-        refiner = true;
-        if (rq == "FP16") rkind = K_FP16;
-        for (const char *u : no_refiner)
-            if (rq == u) refiner = false;
-        if ((rq == "SQ8U" || rq == "SQ8") && factor != 1.0f)
-            return fail(GSX_ERR_UNSUPPORTED, "refine quantizer %s is outside the GPU search path", rq.c_str());
-        if (rq == "SQ8U" || rq == "SQ8") refiner = false;  // factor 1: the refiner only forwards
-    }
-    if (kind == K_SQ1 && !(metric && std::string(metric) == "IP"))  // graph_searcher.hpp:362-369
-        return fail(GSX_ERR_UNSUPPORTED, "SQ1 searchers exist for the IP metric only");
-    auto *s = new gsx_searcher;
-    s->kind = kind;
-    // metric_map (common.hpp:13-19): unknown names fall on the default-constructed L2
-    s->metric = (metric && std::string(metric) == "IP") ? M_IP : M_L2;
-    s->has_refine = (refiner && factor != 1.0f) ? 1 : 0;
-    s->r_kind = rkind;
-    s->refine_factor = factor;
-    s->device = device;
-    s->graph = std::move(graph->g);  // the Python Graph is moved from (python/bindings.cc:98)
-    graph->g = HostGraph();
-    auto bad = [&](int code) {
-        gsx_searcher_destroy(s);
-        return code;
-    };
-    if ((rc = set_device(s))) return bad(rc);
-    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return bad(cuda_fail(e, "cudaStreamCreate"));
-    cudaEventCreate(&s->ev0);
-    cudaEventCreate(&s->ev1);
-    cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device);
-    const HostGraph &g = s->graph;
-    if ((rc = upload(s->adj, g.adj.data(), g.adj.size(), s->stream))) return bad(rc);
-    if ((rc = upload(s->eps, g.eps.data(), g.eps.size(), s->stream))) return bad(rc);
-    if (g.has_hnsw) {
-        if ((rc = upload(s->levels, g.levels.data(), g.levels.size(), s->stream))) return bad(rc);
-        if ((rc = upload(s->loff, g.loff.data(), g.loff.size(), s->stream))) return bad(rc);
-        if ((rc = upload(s->lists, g.lists.data(), std::max<size_t>(g.lists.size(), 1), s->stream))) return bad(rc);
-    }
-    e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return bad(cuda_fail(e, "graph upload"));
-    IndexView &ix = s->ix;
-    ix.N = g.N;
-    ix.K = g.K;
-    ix.adj = s->adj.as<int32_t>();
-    ix.nep = (int32_t)g.eps.size();
-    ix.eps = s->eps.as<int32_t>();
-    ix.has_hnsw = g.has_hnsw;
-    ix.hK = g.hK;
-    ix.hep = g.hep;
-    ix.levels = s->levels.as<int32_t>();
-    ix.loff = s->loff.as<int64_t>();
-    ix.lists = s->lists.as<int32_t>();
-    ix.kind = kind;
-    ix.metric = s->metric;
-    ix.has_refine = s->has_refine;
-    ix.refine_factor = factor;
-    *out = s;
-    return GSX_OK;
+    try {
+        if (!graph || !out) return fail(GSX_ERR_INVALID, "null argument");
+        if (graph->g.N == 0) return fail(GSX_ERR_STATE, "graph is empty (already moved into a searcher?)");
+        int ndev = gsx_device_count();
+        if (ndev == 0) return fail(GSX_ERR_CUDA, "no CUDA device is visible");
+        if (device < 0 || device >= ndev) return fail(GSX_ERR_INVALID, "device %d out of range", device);
+        int kind;
+        int rc = parse_quant(quantizer ? quantizer : "", &kind);
+        if (rc) return rc;
+        const std::string rq = refine_quant ? refine_quant : "";
+        // get_refine_factor (graph_searcher.hpp:227-238): 1.5 for SQ8U/SQ8/SQ4U, 3 for SQ2U, 1.0 otherwise (in which
+        // case the Refiner forwards to the inner searcher unchanged, refiner.hpp:47-50)
+        const float factor = (kind == K_SQ2U || kind == K_SQ1)                                           ? 3.0f
+                             : (kind == K_SQ8U || kind == K_SQ4U || kind == K_SQ8 || kind == K_SQ4UA) ? 1.5f
+                                                                                                      : 1.0f;
+        // make_refiner (graph_searcher.hpp:240-254): FP16 -> FP16 store; FP32 or a name the quantizer map
+        // does not know -> FP32 store; SQ8U / SQ8 -> their own refiners; any other known name -> none
+        int rkind = K_FP32;
+        bool refiner = false;
+        if (!rq.empty()) {
+            static const char *no_refiner[] = {"BF16", "E5M2", "SQ6", "SQ4U", "SQ4UA", "SQ4", "SQ8P", "SQ1", "SQ2U", "PQ8"};
+            refiner = true;
+            if (rq == "FP16") rkind = K_FP16;
+            for (const char *u : no_refiner)
+                if (rq == u) refiner = false;
+            if ((rq == "SQ8U" || rq == "SQ8") && factor != 1.0f)
+                return fail(GSX_ERR_UNSUPPORTED, "refine quantizer %s is outside the GPU search path", rq.c_str());
+            if (rq == "SQ8U" || rq == "SQ8") refiner = false;  // factor 1: the refiner only forwards
+        }
+        if (kind == K_SQ1 && !(metric && std::string(metric) == "IP"))  // graph_searcher.hpp:362-369
+            return fail(GSX_ERR_UNSUPPORTED, "SQ1 searchers exist for the IP metric only");
+        auto *s = new gsx_searcher;
+        s->kind = kind;
+        // metric_map (common.hpp:13-19): unknown names fall on the default-constructed L2
+        s->metric = (metric && std::string(metric) == "IP") ? M_IP : M_L2;
+        s->has_refine = (refiner && factor != 1.0f) ? 1 : 0;
+        s->r_kind = rkind;
+        s->refine_factor = factor;
+        s->device = device;
+        s->graph = std::move(graph->g);  // the Python Graph is moved from (python/bindings.cc:98)
+        graph->g = HostGraph();
+        auto bad = [&](int code) {
+            gsx_searcher_destroy(s);
+            return code;
+        };
+        if ((rc = set_device(s))) return bad(rc);
+        cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return bad(cuda_fail(e, "cudaStreamCreate"));
+        cudaEventCreate(&s->ev0);
+        cudaEventCreate(&s->ev1);
+        cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device);
+        const HostGraph &g = s->graph;
+        if ((rc = upload(s->adj, g.adj.data(), g.adj.size(), s->stream))) return bad(rc);
+        if ((rc = upload(s->eps, g.eps.data(), g.eps.size(), s->stream))) return bad(rc);
+        if (g.has_hnsw) {
+            if ((rc = upload(s->levels, g.levels.data(), g.levels.size(), s->stream))) return bad(rc);
+            if ((rc = upload(s->loff, g.loff.data(), g.loff.size(), s->stream))) return bad(rc);
+            if ((rc = upload(s->lists, g.lists.data(), std::max<size_t>(g.lists.size(), 1), s->stream))) return bad(rc);
+        }
+        e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return bad(cuda_fail(e, "graph upload"));
+        IndexView &ix = s->ix;
+        ix.N = g.N;
+        ix.K = g.K;
+        ix.adj = s->adj.as<int32_t>();
+        ix.nep = (int32_t)g.eps.size();
+        ix.eps = s->eps.as<int32_t>();
+        ix.has_hnsw = g.has_hnsw;
+        ix.hK = g.hK;
+        ix.hep = g.hep;
+        ix.levels = s->levels.as<int32_t>();
+        ix.loff = s->loff.as<int64_t>();
+        ix.lists = s->lists.as<int32_t>();
+        ix.kind = kind;
+        ix.metric = s->metric;
+        ix.has_refine = s->has_refine;
+        ix.refine_factor = factor;
+        *out = s;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_create")
 }
 
 void gsx_searcher_destroy(gsx_searcher *s) {
@@ -695,281 +701,313 @@ void gsx_searcher_destroy(gsx_searcher *s) {
 }
 
 int gsx_searcher_set_data(gsx_searcher *s, const float *data, int32_t n, int32_t dim) {
-    if (!s || !data) return fail(GSX_ERR_INVALID, "null argument");
-    if (dim <= 0 || n <= 0) return fail(GSX_ERR_INVALID, "bad data shape %d x %d", n, dim);
-    if (n < s->ix.N) return fail(GSX_ERR_INVALID, "data has %d rows but the graph has %d nodes", n, s->ix.N);
-    int rc = set_device(s);
-    if (rc) return rc;
-    IndexView &ix = s->ix;
-    ix.d = dim;
-    layout(s->kind, dim, &ix.dalign, &ix.csize);
-    cudaStream_t st = s->stream;
-    DevBuf raw, scratch;
-    if ((rc = upload(raw, data, (size_t)n * dim, st))) return rc;
-    float p[2];
-    if ((rc = calibrate(s->kind, s->metric, raw.as<float>(), n, dim, p, scratch, st))) return rc;
-    ix.p0 = p[0];
-    ix.p1 = p[1];
-    if ((rc = s->codes.ensure((size_t)n * ix.csize))) return rc;
-    ix.sq8p = nullptr;
-    if (s->kind == K_FP32) {
-        GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.dalign, s->codes.as<float>(), st));
-    } else if (s->kind == K_SQ8) {
-        // the per-dimension calibrator trained and applied on the device (calib_kernel.cu)
-        if ((rc = s->sq8p.ensure((size_t)2 * ix.dalign * 4))) return rc;
-        GSX_CUDA(launch_block_minmax(raw.as<float>(), n, dim, ix.dalign, s->sq8p.as<float>(), st));
-        GSX_CUDA(launch_encode_sq8(raw.as<float>(), n, dim, ix.dalign, s->sq8p.as<float>(), s->codes.as<uint8_t>(), st));
-        s->h_sq8p.resize((size_t)2 * ix.dalign);
-        GSX_CUDA(cudaMemcpyAsync(s->h_sq8p.data(), s->sq8p.p, s->h_sq8p.size() * 4, cudaMemcpyDeviceToHost, st));
-        ix.sq8p = s->sq8p.as<float>();
-    } else {
-        GSX_CUDA(launch_encode(s->kind, s->metric, raw.as<float>(), n, dim, ix.dalign, ix.csize, ix.p0, ix.p1,
-                               s->codes.as<uint8_t>(), st));
-    }
-    if (s->has_refine) {
-        ix.r_dalign = (dim + 15) / 16 * 16;
-        if (s->r_kind == K_FP16) {
-            if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 2))) return rc;
-            GSX_CUDA(launch_encode(K_FP16, s->metric, raw.as<float>(), n, dim, ix.r_dalign, ix.r_dalign * 2, 0.0f, 0.0f,
-                                   s->r_codes.as<uint8_t>(), st));
+    try {
+        if (!s || !data) return fail(GSX_ERR_INVALID, "null argument");
+        if (dim <= 0 || n <= 0) return fail(GSX_ERR_INVALID, "bad data shape %d x %d", n, dim);
+        if (n < s->ix.N) return fail(GSX_ERR_INVALID, "data has %d rows but the graph has %d nodes", n, s->ix.N);
+        int rc = set_device(s);
+        if (rc) return rc;
+        IndexView &ix = s->ix;
+        ix.d = dim;
+        layout(s->kind, dim, &ix.dalign, &ix.csize);
+        cudaStream_t st = s->stream;
+        DevBuf raw, scratch;
+        if ((rc = upload(raw, data, (size_t)n * dim, st))) return rc;
+        float p[2];
+        if ((rc = calibrate(s->kind, s->metric, raw.as<float>(), n, dim, p, scratch, st))) return rc;
+        ix.p0 = p[0];
+        ix.p1 = p[1];
+        if ((rc = s->codes.ensure((size_t)n * ix.csize))) return rc;
+        ix.sq8p = nullptr;
+        if (s->kind == K_FP32) {
+            GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.dalign, s->codes.as<float>(), st));
+        } else if (s->kind == K_SQ8) {
+            // the per-dimension calibrator trained and applied on the device (calib_kernel.cu)
+            if ((rc = s->sq8p.ensure((size_t)2 * ix.dalign * 4))) return rc;
+            GSX_CUDA(launch_block_minmax(raw.as<float>(), n, dim, ix.dalign, s->sq8p.as<float>(), st));
+            GSX_CUDA(launch_encode_sq8(raw.as<float>(), n, dim, ix.dalign, s->sq8p.as<float>(), s->codes.as<uint8_t>(), st));
+            s->h_sq8p.resize((size_t)2 * ix.dalign);
+            GSX_CUDA(cudaMemcpyAsync(s->h_sq8p.data(), s->sq8p.p, s->h_sq8p.size() * 4, cudaMemcpyDeviceToHost, st));
+            ix.sq8p = s->sq8p.as<float>();
         } else {
-            if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 4))) return rc;
-            GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.r_dalign, s->r_codes.as<float>(), st));
+            GSX_CUDA(launch_encode(s->kind, s->metric, raw.as<float>(), n, dim, ix.dalign, ix.csize, ix.p0, ix.p1,
+                                   s->codes.as<uint8_t>(), st));
         }
-    }
-    GSX_CUDA(cudaStreamSynchronize(st));
-    ix.codes = s->codes.as<uint8_t>();
-    ix.r_codes = s->r_codes.as<uint8_t>();
-    ix.r_kind = s->r_kind;
-    // keep 1,000 sampled rows for optimize (graph_searcher.hpp:62-69)
-    s->sample_n = std::min(1000, n);
-    std::mt19937 rng(12345);
-    s->sample.resize((size_t)s->sample_n * dim);
-    for (int i = 0; i < s->sample_n; ++i) {
-        const int r = (int)(rng() % (uint32_t)n);
-        std::memcpy(&s->sample[(size_t)i * dim], data + (size_t)r * dim, (size_t)dim * 4);
-    }
-    if ((rc = batch_order_setup(s))) return rc;
-    s->has_data = true;
-    return GSX_OK;
+        if (s->has_refine) {
+            ix.r_dalign = (dim + 15) / 16 * 16;
+            if (s->r_kind == K_FP16) {
+                if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 2))) return rc;
+                GSX_CUDA(launch_encode(K_FP16, s->metric, raw.as<float>(), n, dim, ix.r_dalign, ix.r_dalign * 2, 0.0f, 0.0f,
+                                       s->r_codes.as<uint8_t>(), st));
+            } else {
+                if ((rc = s->r_codes.ensure((size_t)n * ix.r_dalign * 4))) return rc;
+                GSX_CUDA(launch_pad_rows(raw.as<float>(), n, dim, ix.r_dalign, s->r_codes.as<float>(), st));
+            }
+        }
+        GSX_CUDA(cudaStreamSynchronize(st));
+        ix.codes = s->codes.as<uint8_t>();
+        ix.r_codes = s->r_codes.as<uint8_t>();
+        ix.r_kind = s->r_kind;
+        // keep 1,000 sampled rows for optimize (graph_searcher.hpp:62-69)
+        s->sample_n = std::min(1000, n);
+        std::mt19937 rng(12345);
+        s->sample.resize((size_t)s->sample_n * dim);
+        for (int i = 0; i < s->sample_n; ++i) {
+            const int r = (int)(rng() % (uint32_t)n);
+            std::memcpy(&s->sample[(size_t)i * dim], data + (size_t)r * dim, (size_t)dim * 4);
+        }
+        if ((rc = batch_order_setup(s))) return rc;
+        s->has_data = true;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_set_data")
 }
 
 int gsx_searcher_set_ef(gsx_searcher *s, int32_t ef) {
-    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
-    if (ef <= 0) return fail(GSX_ERR_INVALID, "ef must be positive");
-    s->ef = ef;
-    return GSX_OK;
+    try {
+        if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+        if (ef <= 0) return fail(GSX_ERR_INVALID, "ef must be positive");
+        s->ef = ef;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_set_ef")
 }
 
 int gsx_searcher_get_ef(const gsx_searcher *s, int32_t *ef) {
-    if (!s || !ef) return fail(GSX_ERR_INVALID, "null argument");
-    *ef = s->ef;
-    return GSX_OK;
+    try {
+        if (!s || !ef) return fail(GSX_ERR_INVALID, "null argument");
+        *ef = s->ef;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_get_ef")
 }
 
 int gsx_searcher_search(gsx_searcher *s, const float *query, int32_t k, int32_t *ids, float *dis) {
-    if (!s || !query || !ids) return fail(GSX_ERR_INVALID, "null argument");
-    return host_batch(s, query, 1, k, nullptr, nullptr, k, ids, dis, true);
+    try {
+        if (!s || !query || !ids) return fail(GSX_ERR_INVALID, "null argument");
+        return host_batch(s, query, 1, k, nullptr, nullptr, k, ids, dis, true);
+    } GSX_ABI_GUARD("gsx_searcher_search")
 }
 
 int gsx_searcher_search_batch(gsx_searcher *s, const float *queries, int32_t nq, int32_t k, int32_t *ids, float *dis) {
-    if (!s || (nq > 0 && (!queries || !ids))) return fail(GSX_ERR_INVALID, "null argument");
-    return host_batch(s, queries, nq, k, nullptr, nullptr, k, ids, dis, false);
+    try {
+        if (!s || (nq > 0 && (!queries || !ids))) return fail(GSX_ERR_INVALID, "null argument");
+        return host_batch(s, queries, nq, k, nullptr, nullptr, k, ids, dis, false);
+    } GSX_ABI_GUARD("gsx_searcher_search_batch")
 }
 
 int gsx_searcher_search_batch_mixed(gsx_searcher *s, const float *queries, int32_t nq, int32_t k, const int32_t *ef,
                                     const int32_t *kq, int32_t kmax, int32_t *ids, float *dis) {
-    if (!s || (nq > 0 && (!queries || !ids))) return fail(GSX_ERR_INVALID, "null argument");
-    if (kq && kmax <= 0) return fail(GSX_ERR_INVALID, "kmax required with per-query k");
-    if (!kq) kmax = k;
-    return host_batch(s, queries, nq, k, ef, kq, kmax, ids, dis, false);
+    try {
+        if (!s || (nq > 0 && (!queries || !ids))) return fail(GSX_ERR_INVALID, "null argument");
+        if (kq && kmax <= 0) return fail(GSX_ERR_INVALID, "kmax required with per-query k");
+        if (!kq) kmax = k;
+        return host_batch(s, queries, nq, k, ef, kq, kmax, ids, dis, false);
+    } GSX_ABI_GUARD("gsx_searcher_search_batch_mixed")
 }
 
 int gsx_searcher_search_batch_device(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
                                      const int32_t *d_ef, const int32_t *d_k, int32_t kmax, int32_t *d_ids,
                                      float *d_dis, int32_t *d_cmps, int32_t *d_expansions, void *stream) {
-    if (!s || (nq > 0 && (!d_queries || !d_ids))) return fail(GSX_ERR_INVALID, "null argument");
-    if (!s->has_data) return fail(GSX_ERR_STATE, "search before set_data");
-    if (k <= 0) return fail(GSX_ERR_INVALID, "k must be positive");
-    if (kmax < k) kmax = k;
-    int rc = set_device(s);
-    if (rc) return rc;
-    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
-    // with per-query ef on the device the caller's searcher ef is the upper bound
-    return enqueue(s, d_queries, nq, k, s->ef, d_ef, d_k, kmax, s->ef, d_ids, d_dis, d_cmps, false, st, nullptr,
-                   d_expansions);
+    try {
+        if (!s || (nq > 0 && (!d_queries || !d_ids))) return fail(GSX_ERR_INVALID, "null argument");
+        if (!s->has_data) return fail(GSX_ERR_STATE, "search before set_data");
+        if (k <= 0) return fail(GSX_ERR_INVALID, "k must be positive");
+        if (kmax < k) kmax = k;
+        int rc = set_device(s);
+        if (rc) return rc;
+        cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+        // with per-query ef on the device the caller's searcher ef is the upper bound
+        return enqueue(s, d_queries, nq, k, s->ef, d_ef, d_k, kmax, s->ef, d_ids, d_dis, d_cmps, false, st, nullptr,
+                       d_expansions);
+    } GSX_ABI_GUARD("gsx_searcher_search_batch_device")
 }
 
 int gsx_searcher_get_last_search_avg_dist_cmps(const gsx_searcher *s, double *out) {
-    if (!s || !out) return fail(GSX_ERR_INVALID, "null argument");
-    *out = s->last_avg_cmps;
-    return GSX_OK;
+    try {
+        if (!s || !out) return fail(GSX_ERR_INVALID, "null argument");
+        *out = s->last_avg_cmps;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_get_last_search_avg_dist_cmps")
 }
 
 int gsx_searcher_get_tuning(const gsx_searcher *s, gsx_tuning *t) {
-    if (!s || !t) return fail(GSX_ERR_INVALID, "null argument");
-    *t = s->tuning;
-    return GSX_OK;
+    try {
+        if (!s || !t) return fail(GSX_ERR_INVALID, "null argument");
+        *t = s->tuning;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_get_tuning")
 }
 
 int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
-    if (!s || !t) return fail(GSX_ERR_INVALID, "null argument");
-    if (t->warps_per_block < 0 || t->warps_per_block > 8 || (t->warps_per_block & (t->warps_per_block - 1)))
-        return fail(GSX_ERR_INVALID, "warps_per_block must be 0 or a power of two <= 8");
-    if (t->lanes_per_row != 0 && t->lanes_per_row != 1 && t->lanes_per_row != 2 && t->lanes_per_row != 4)
-        return fail(GSX_ERR_INVALID, "lanes_per_row must be 0, 1, 2 or 4");
-    if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
-        return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
-                    kMinTableBits);
-    if (t->prefetch < 0 || t->prefetch > 31) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 31]");
-    if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
-        return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
-    s->tuning = *t;
-    if (is_float_kind(s->kind) && s->tuning.lanes_per_row == 2) s->tuning.lanes_per_row = 4;
-    return GSX_OK;
+    try {
+        if (!s || !t) return fail(GSX_ERR_INVALID, "null argument");
+        if (t->warps_per_block < 0 || t->warps_per_block > 8 || (t->warps_per_block & (t->warps_per_block - 1)))
+            return fail(GSX_ERR_INVALID, "warps_per_block must be 0 or a power of two <= 8");
+        if (t->lanes_per_row != 0 && t->lanes_per_row != 1 && t->lanes_per_row != 2 && t->lanes_per_row != 4)
+            return fail(GSX_ERR_INVALID, "lanes_per_row must be 0, 1, 2 or 4");
+        if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
+            return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
+                        kMinTableBits);
+        if (t->prefetch < 0 || t->prefetch > 31) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 31]");
+        if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
+            return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
+        s->tuning = *t;
+        if (is_float_kind(s->kind) && s->tuning.lanes_per_row == 2) s->tuning.lanes_per_row = 4;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_set_tuning")
 }
 
 int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
-    (void)num_threads;
-    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
-    if (!s->has_data) return fail(GSX_ERR_STATE, "optimize before set_data");
-    int rc = set_device(s);
-    if (rc) return rc;
-    // the sample is tiled to enough queries to fill the GPU several times over, so that the timing
-    // measures throughput (a single wave would only measure the slowest query's latency)
-    const int reps = std::max(1, (16384 + s->sample_n - 1) / s->sample_n);
-    const int nq = s->sample_n * reps, k = 10, d = s->ix.d;
-    cudaStream_t st = s->stream;
-    std::vector<float> tiled((size_t)nq * d);
-    for (int r = 0; r < reps; ++r)
-        std::memcpy(tiled.data() + (size_t)r * s->sample_n * d, s->sample.data(), (size_t)s->sample_n * d * 4);
-    if ((rc = upload(s->q, tiled.data(), (size_t)nq * d, st))) return rc;
-    if ((rc = s->ids.ensure((size_t)nq * k * 4))) return rc;
-    if ((rc = s->dis.ensure((size_t)nq * k * 4))) return rc;
-    const gsx_tuning saved = s->tuning;
-    const int base_bits = default_table_bits(s, std::max(s->ef, kin_of(s, k)));
-    std::vector<int> lprs = is_float_kind(s->kind) ? std::vector<int>{1, 4} : std::vector<int>{1, 2, 4};
-    gsx_tuning best = saved;
-    float best_ms = 1e30f;
-    // visited sets in global tables only, or a small shared table in front; sparse global tables
-    std::vector<int> bit_choices{kGlobalOnly, 9};
-    (void)base_bits;
-    const int sb0 = s->tuning.spill_bits;
-    s->tuning.spill_bits = 0;
-    LaunchCfg probe;
-    int auto_sb = 14;
-    if (make_cfg(s, k, s->ef, nq, false, 0, &probe) == GSX_OK) auto_sb = spill_bits_for(s, probe);
-    s->tuning.spill_bits = sb0;
-    for (int wpb : {2, 4})
-        for (int lpr : lprs)
-            for (int bits : bit_choices)
-            for (int pf : {0, 4})
-            for (int sb : {auto_sb, auto_sb + 1}) {
-                gsx_tuning t{wpb, bits, lpr, pf, sb};
-                s->tuning = t;
-                float ms_min = 1e30f;
-                bool ok = true;
-                for (int rep = 0; rep < 3 && ok; ++rep) {
-                    cudaEventRecord(s->ev0, st);
-                    rc = enqueue(s, s->q.as<float>(), nq, k, s->ef, nullptr, nullptr, k, s->ef, s->ids.as<int32_t>(),
-                                 s->dis.as<float>(), nullptr, false, st);
-                    if (rc) { ok = false; break; }
-                    cudaEventRecord(s->ev1, st);
-                    unsigned nover = 0;
-                    cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st);
-                    if (cudaStreamSynchronize(st) != cudaSuccess) {
-                        s->tuning = saved;
-                        return cuda_fail(cudaGetLastError(), "optimize");
+    try {
+        (void)num_threads;
+        if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+        if (!s->has_data) return fail(GSX_ERR_STATE, "optimize before set_data");
+        int rc = set_device(s);
+        if (rc) return rc;
+        // the sample is tiled to enough queries to fill the GPU several times over, so that the timing
+        // measures throughput (a single wave would only measure the slowest query's latency)
+        const int reps = std::max(1, (16384 + s->sample_n - 1) / s->sample_n);
+        const int nq = s->sample_n * reps, k = 10, d = s->ix.d;
+        cudaStream_t st = s->stream;
+        std::vector<float> tiled((size_t)nq * d);
+        for (int r = 0; r < reps; ++r)
+            std::memcpy(tiled.data() + (size_t)r * s->sample_n * d, s->sample.data(), (size_t)s->sample_n * d * 4);
+        if ((rc = upload(s->q, tiled.data(), (size_t)nq * d, st))) return rc;
+        if ((rc = s->ids.ensure((size_t)nq * k * 4))) return rc;
+        if ((rc = s->dis.ensure((size_t)nq * k * 4))) return rc;
+        const gsx_tuning saved = s->tuning;
+        const int base_bits = default_table_bits(s, std::max(s->ef, kin_of(s, k)));
+        std::vector<int> lprs = is_float_kind(s->kind) ? std::vector<int>{1, 4} : std::vector<int>{1, 2, 4};
+        gsx_tuning best = saved;
+        float best_ms = 1e30f;
+        // visited sets in global tables only, or a small shared table in front; sparse global tables
+        std::vector<int> bit_choices{kGlobalOnly, 9};
+        (void)base_bits;
+        const int sb0 = s->tuning.spill_bits;
+        s->tuning.spill_bits = 0;
+        LaunchCfg probe;
+        int auto_sb = 14;
+        if (make_cfg(s, k, s->ef, nq, false, 0, &probe) == GSX_OK) auto_sb = spill_bits_for(s, probe);
+        s->tuning.spill_bits = sb0;
+        for (int wpb : {2, 4})
+            for (int lpr : lprs)
+                for (int bits : bit_choices)
+                for (int pf : {0, 4})
+                for (int sb : {auto_sb, auto_sb + 1}) {
+                    gsx_tuning t{wpb, bits, lpr, pf, sb};
+                    s->tuning = t;
+                    float ms_min = 1e30f;
+                    bool ok = true;
+                    for (int rep = 0; rep < 3 && ok; ++rep) {
+                        cudaEventRecord(s->ev0, st);
+                        rc = enqueue(s, s->q.as<float>(), nq, k, s->ef, nullptr, nullptr, k, s->ef, s->ids.as<int32_t>(),
+                                     s->dis.as<float>(), nullptr, false, st);
+                        if (rc) { ok = false; break; }
+                        cudaEventRecord(s->ev1, st);
+                        unsigned nover = 0;
+                        cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st);
+                        if (cudaStreamSynchronize(st) != cudaSuccess) {
+                            s->tuning = saved;
+                            return cuda_fail(cudaGetLastError(), "optimize");
+                        }
+                        if (nover) { ok = false; break; }  // a table that overflows is not a candidate
+                        float ms = 0;
+                        cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+                        ms_min = std::min(ms_min, ms);
                     }
-                    if (nover) { ok = false; break; }  // a table that overflows is not a candidate
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-                    ms_min = std::min(ms_min, ms);
+                    if (ok && ms_min < best_ms) {
+                        best_ms = ms_min;
+                        best = t;
+                    }
                 }
-                if (ok && ms_min < best_ms) {
-                    best_ms = ms_min;
-                    best = t;
-                }
-            }
-    s->tuning = best;
-    return GSX_OK;
+        s->tuning = best;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_optimize")
 }
 
 int gsx_searcher_memory(const gsx_searcher *s, size_t *index_bytes, size_t *per_query_bytes) {
-    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
-    if (index_bytes)
-        *index_bytes = s->adj.bytes + s->eps.bytes + s->levels.bytes + s->loff.bytes + s->lists.bytes + s->codes.bytes +
-                       s->r_codes.bytes + s->sq8p.bytes;
-    if (per_query_bytes) {
-        // device bytes one in-flight query holds outside the resident index: its fp32 row,
-        // outputs (k up to 256), status and counter
-        *per_query_bytes = (size_t)s->ix.d * 4 + 256 * 8 + 16;
-    }
-    return GSX_OK;
+    try {
+        if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+        if (index_bytes)
+            *index_bytes = s->adj.bytes + s->eps.bytes + s->levels.bytes + s->loff.bytes + s->lists.bytes + s->codes.bytes +
+                           s->r_codes.bytes + s->sq8p.bytes;
+        if (per_query_bytes) {
+            // device bytes one in-flight query holds outside the resident index: its fp32 row,
+            // outputs (k up to 256), status and counter
+            *per_query_bytes = (size_t)s->ix.d * 4 + 256 * 8 + 16;
+        }
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_memory")
 }
 
 int gsx_searcher_distances(gsx_searcher *s, const float *queries, int32_t nq, const int32_t *ids, int32_t m,
                            int32_t refine, double *out) {
-    if (!s || !queries || !ids || !out) return fail(GSX_ERR_INVALID, "null argument");
-    if (!s->has_data) return fail(GSX_ERR_STATE, "distances before set_data");
-    if (refine && !s->has_refine) return fail(GSX_ERR_STATE, "searcher has no refine store");
-    for (int64_t i = 0; i < (int64_t)nq * m; ++i)
-        if (ids[i] < 0 || ids[i] >= s->ix.N) return fail(GSX_ERR_INVALID, "id %d out of range", ids[i]);
-    int rc = set_device(s);
-    if (rc) return rc;
-    cudaStream_t st = s->stream;
-    if ((rc = upload(s->q, queries, (size_t)nq * s->ix.d, st))) return rc;
-    if ((rc = upload(s->dist_ids, ids, (size_t)nq * m, st))) return rc;
-    if ((rc = s->dist_out.ensure((size_t)nq * m * 8))) return rc;
-    GSX_CUDA(launch_distances(s->ix, refine, s->q.as<float>(), nq, s->dist_ids.as<int32_t>(), m,
-                              s->dist_out.as<double>(), st));
-    GSX_CUDA(cudaMemcpyAsync(out, s->dist_out.p, (size_t)nq * m * 8, cudaMemcpyDeviceToHost, st));
-    GSX_CUDA(cudaStreamSynchronize(st));
-    return GSX_OK;
+    try {
+        if (!s || !queries || !ids || !out) return fail(GSX_ERR_INVALID, "null argument");
+        if (!s->has_data) return fail(GSX_ERR_STATE, "distances before set_data");
+        if (refine && !s->has_refine) return fail(GSX_ERR_STATE, "searcher has no refine store");
+        for (int64_t i = 0; i < (int64_t)nq * m; ++i)
+            if (ids[i] < 0 || ids[i] >= s->ix.N) return fail(GSX_ERR_INVALID, "id %d out of range", ids[i]);
+        int rc = set_device(s);
+        if (rc) return rc;
+        cudaStream_t st = s->stream;
+        if ((rc = upload(s->q, queries, (size_t)nq * s->ix.d, st))) return rc;
+        if ((rc = upload(s->dist_ids, ids, (size_t)nq * m, st))) return rc;
+        if ((rc = s->dist_out.ensure((size_t)nq * m * 8))) return rc;
+        GSX_CUDA(launch_distances(s->ix, refine, s->q.as<float>(), nq, s->dist_ids.as<int32_t>(), m,
+                                  s->dist_out.as<double>(), st));
+        GSX_CUDA(cudaMemcpyAsync(out, s->dist_out.p, (size_t)nq * m * 8, cudaMemcpyDeviceToHost, st));
+        GSX_CUDA(cudaStreamSynchronize(st));
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_distances")
 }
 
 int gsx_searcher_codes(const gsx_searcher *s, uint8_t *codes, float *params, int32_t *code_size) {
-    if (!s) return fail(GSX_ERR_INVALID, "null searcher");
-    if (!s->has_data) return fail(GSX_ERR_STATE, "codes before set_data");
-    if (code_size) *code_size = s->ix.csize;
-    if (params) {
-        const bool sq8 = s->kind == K_SQ8 && !s->h_sq8p.empty();
-        params[0] = sq8 ? s->h_sq8p[0] : s->ix.p0;
-        params[1] = sq8 ? s->h_sq8p[s->h_sq8p.size() / 2] : s->ix.p1;
-    }
-    if (codes) {
-        int rc = set_device(s);
-        if (rc) return rc;
-        GSX_CUDA(cudaMemcpy(codes, s->codes.p, (size_t)s->ix.N * s->ix.csize, cudaMemcpyDeviceToHost));
-    }
-    return GSX_OK;
+    try {
+        if (!s) return fail(GSX_ERR_INVALID, "null searcher");
+        if (!s->has_data) return fail(GSX_ERR_STATE, "codes before set_data");
+        if (code_size) *code_size = s->ix.csize;
+        if (params) {
+            const bool sq8 = s->kind == K_SQ8 && !s->h_sq8p.empty();
+            params[0] = sq8 ? s->h_sq8p[0] : s->ix.p0;
+            params[1] = sq8 ? s->h_sq8p[s->h_sq8p.size() / 2] : s->ix.p1;
+        }
+        if (codes) {
+            int rc = set_device(s);
+            if (rc) return rc;
+            GSX_CUDA(cudaMemcpy(codes, s->codes.p, (size_t)s->ix.N * s->ix.csize, cudaMemcpyDeviceToHost));
+        }
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_codes")
 }
 
 int gsx_searcher_params(const gsx_searcher *s, float *params, int32_t *count) {
-    if (!s || !count) return fail(GSX_ERR_INVALID, "null argument");
-    if (!s->has_data) return fail(GSX_ERR_STATE, "params before set_data");
-    if (s->kind == K_SQ8) {
-        *count = (int32_t)s->h_sq8p.size();
-        if (params) std::memcpy(params, s->h_sq8p.data(), s->h_sq8p.size() * 4);
-    } else {
-        *count = 2;
-        if (params) {
-            params[0] = s->ix.p0;
-            params[1] = s->ix.p1;
+    try {
+        if (!s || !count) return fail(GSX_ERR_INVALID, "null argument");
+        if (!s->has_data) return fail(GSX_ERR_STATE, "params before set_data");
+        if (s->kind == K_SQ8) {
+            *count = (int32_t)s->h_sq8p.size();
+            if (params) std::memcpy(params, s->h_sq8p.data(), s->h_sq8p.size() * 4);
+        } else {
+            *count = 2;
+            if (params) {
+                params[0] = s->ix.p0;
+                params[1] = s->ix.p1;
+            }
         }
-    }
-    return GSX_OK;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_params")
 }
 
 int gsx_searcher_overflow_count(gsx_searcher *s, uint32_t *count) {
-    if (!s || !count) return fail(GSX_ERR_INVALID, "null argument");
-    *count = 0;
-    if (!s->counters.p) return GSX_OK;
-    int rc = set_device(s);
-    if (rc) return rc;
-    GSX_CUDA(cudaMemcpyAsync(count, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, s->stream));
-    GSX_CUDA(cudaStreamSynchronize(s->stream));
-    return GSX_OK;
+    try {
+        if (!s || !count) return fail(GSX_ERR_INVALID, "null argument");
+        *count = 0;
+        if (!s->counters.p) return GSX_OK;
+        int rc = set_device(s);
+        if (rc) return rc;
+        GSX_CUDA(cudaMemcpyAsync(count, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, s->stream));
+        GSX_CUDA(cudaStreamSynchronize(s->stream));
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_overflow_count")
 }
 
 }  // extern "C"

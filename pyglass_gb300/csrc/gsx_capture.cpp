@@ -130,63 +130,71 @@ extern "C" int gsx_searcher_capture_batch(gsx_searcher *s, const float *d_querie
                                           const int32_t *d_ef, const int32_t *d_k, int32_t kmax, int32_t *d_ids,
                                           float *d_dis, int32_t *d_cmps, int32_t *d_expansions,
                                           gsx_batch_graph **out) {
-    if (!out) return fail(GSX_ERR_INVALID, "null argument");
-    *out = nullptr;
-    if (!s || !d_queries || !d_ids || !d_dis) return fail(GSX_ERR_INVALID, "null argument");
-    if (!s->has_data) return fail(GSX_ERR_STATE, "search before set_data");
-    if (nq <= 0) return fail(GSX_ERR_INVALID, "a captured batch needs at least one query");
-    if (k <= 0) return fail(GSX_ERR_INVALID, "k must be positive");
-    if (kmax < k) kmax = k;
-    cudaError_t e = cudaSetDevice(s->device);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
-    gsx_batch_graph *g = new (std::nothrow) gsx_batch_graph;
-    if (!g) return fail(GSX_ERR_NOMEM, "out of host memory");
-    g->s = s;
-    g->device = s->device;
-    g->q = d_queries;
-    g->nq = nq;
-    g->k = k;
-    g->kmax = kmax;
-    g->ef = s->ef;  // with per-query ef on the device the searcher's ef is the upper bound
-    g->ef_per = d_ef;
-    g->k_per = d_k;
-    g->ids = d_ids;
-    g->dis = d_dis;
-    g->cmps = d_cmps;
-    g->exps = d_expansions;
-    const int rc = make_graph(g);
-    if (rc) {
-        delete g;
-        return rc;
-    }
-    *out = g;
-    return GSX_OK;
+    try {
+        if (!out) return fail(GSX_ERR_INVALID, "null argument");
+        *out = nullptr;
+        if (!s || !d_queries || !d_ids || !d_dis) return fail(GSX_ERR_INVALID, "null argument");
+        if (!s->has_data) return fail(GSX_ERR_STATE, "search before set_data");
+        if (nq <= 0) return fail(GSX_ERR_INVALID, "a captured batch needs at least one query");
+        if (k <= 0) return fail(GSX_ERR_INVALID, "k must be positive");
+        if (kmax < k) kmax = k;
+        cudaError_t e = cudaSetDevice(s->device);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+        gsx_batch_graph *g = new (std::nothrow) gsx_batch_graph;
+        if (!g) return fail(GSX_ERR_NOMEM, "out of host memory");
+        g->s = s;
+        g->device = s->device;
+        g->q = d_queries;
+        g->nq = nq;
+        g->k = k;
+        g->kmax = kmax;
+        g->ef = s->ef;  // with per-query ef on the device the searcher's ef is the upper bound
+        g->ef_per = d_ef;
+        g->k_per = d_k;
+        g->ids = d_ids;
+        g->dis = d_dis;
+        g->cmps = d_cmps;
+        g->exps = d_expansions;
+        const int rc = make_graph(g);
+        if (rc) {
+            delete g;
+            return rc;
+        }
+        *out = g;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_searcher_capture_batch")
 }
 
 extern "C" int gsx_batch_graph_launch(gsx_batch_graph *g, void *stream) {
-    if (!g || !g->exec) return fail(GSX_ERR_INVALID, "null argument");
-    cudaError_t e = cudaSetDevice(g->device);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
-    cudaStream_t st = stream ? (cudaStream_t)stream : g->s->stream;
-    e = cudaGraphLaunch(g->exec, st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
-    e = cudaEventRecord(g->done, st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
-    return GSX_OK;
+    try {
+        if (!g || !g->exec) return fail(GSX_ERR_INVALID, "null argument");
+        cudaError_t e = cudaSetDevice(g->device);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+        cudaStream_t st = stream ? (cudaStream_t)stream : g->s->stream;
+        e = cudaGraphLaunch(g->exec, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+        e = cudaEventRecord(g->done, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_batch_graph_launch")
 }
 
 extern "C" int gsx_batch_graph_overflow_count(gsx_batch_graph *g, uint32_t *count) {
-    if (!g || !count) return fail(GSX_ERR_INVALID, "null argument");
-    cudaError_t e = cudaSetDevice(g->device);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
-    if ((e = cudaEventSynchronize(g->done)) != cudaSuccess) return cuda_fail(e, "cudaEventSynchronize");
-    if ((e = cudaMemcpy(count, g->counters.as<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost)) != cudaSuccess)
-        return cuda_fail(e, "cudaMemcpy(overflow count)");
-    return GSX_OK;
+    try {
+        if (!g || !count) return fail(GSX_ERR_INVALID, "null argument");
+        cudaError_t e = cudaSetDevice(g->device);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+        if ((e = cudaEventSynchronize(g->done)) != cudaSuccess) return cuda_fail(e, "cudaEventSynchronize");
+        if ((e = cudaMemcpy(count, g->counters.as<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpy(overflow count)");
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_batch_graph_overflow_count")
 }
 
 extern "C" int gsx_batch_graph_destroy(gsx_batch_graph *g) {
-    if (!g) return GSX_OK;
-    delete g;  // waits for the latest launch first
-    return GSX_OK;
+    try {
+        if (!g) return GSX_OK;
+        delete g;  // waits for the latest launch first
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_batch_graph_destroy")
 }

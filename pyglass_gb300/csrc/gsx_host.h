@@ -5,6 +5,8 @@
 
 #include <cstdarg>
 #include <cstdint>
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -17,6 +19,17 @@ namespace gsx {
 int fail(int code, const char *fmt, ...);
 // Maps a CUDA error to GSX_ERR_CUDA / GSX_ERR_NOMEM with a message.
 int cuda_fail(cudaError_t e, const char *what);
+
+// Closes the try block that encloses the body of every int-returning C-ABI entry point, so that
+// no C++ exception crosses the ABI: a failed host allocation becomes GSX_ERR_NOMEM, any other
+// exception GSX_ERR_INVALID, each with a message.
+#define GSX_ABI_GUARD(name)                                                       \
+    catch (const std::bad_alloc &) {                                              \
+        return ::gsx::fail(GSX_ERR_NOMEM, "%s: out of host memory", name);       \
+    }                                                                             \
+    catch (const std::exception &e_) {                                            \
+        return ::gsx::fail(GSX_ERR_INVALID, "%s: %s", name, e_.what());          \
+    }
 
 #define GSX_CUDA(call)                                              \
     do {                                                            \

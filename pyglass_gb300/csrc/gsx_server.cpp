@@ -307,187 +307,199 @@ extern "C" {
 
 int gsx_server_create(gsx_searcher *s, int32_t max_queries_in_flight, int32_t kmax, int32_t efmax, int32_t streams,
                       gsx_server **out) {
-    if (!s || !out) return fail(GSX_ERR_INVALID, "null argument");
-    if (!s->has_data) return fail(GSX_ERR_STATE, "server before set_data");
-    if (max_queries_in_flight <= 0 || kmax <= 0 || efmax <= 0 || streams <= 0 || streams > 32)
-        return fail(GSX_ERR_INVALID, "bad server arguments");
-    int rc;
-    GSX_CUDA(cudaSetDevice(s->device));
-    auto *sv = new gsx_server;
-    sv->s = s;
-    sv->kcap = kmax;
-    sv->efcap = efmax;
-    sv->nstreams = streams;
-    sv->d = s->ix.d;
-    // memory-based admission: the slot arena is sized so that it takes at most half of the free
-    // device memory
-    const size_t per_slot = (size_t)sv->d * 4 + (size_t)kmax * 8 + 16 + (size_t)streams * 4;
-    size_t free_b = 0, total_b = 0;
-    cudaMemGetInfo(&free_b, &total_b);
-    size_t cap = (size_t)max_queries_in_flight;
-    if (per_slot * cap > free_b / 2) cap = std::max<size_t>(1, free_b / 2 / per_slot);
-    sv->capacity = (int)cap;
-    sv->max_group = std::max(256, sv->capacity / (2 * streams));
-    auto bad = [&](int code) {
-        gsx_server_destroy(sv);
-        return code;
-    };
-    if ((rc = sv->dq.ensure(cap * sv->d * 4)) || (rc = sv->dids.ensure(cap * kmax * 4)) ||
-        (rc = sv->ddis.ensure(cap * kmax * 4)) || (rc = sv->dk.ensure(cap * 4)) || (rc = sv->def.ensure(cap * 4)) ||
-        (rc = sv->dstatus.ensure(cap * 4)) || (rc = sv->dorder.ensure(cap * 4 * streams)) ||
-        (rc = sv->dcnt.ensure(64 * streams)))
-        return bad(rc);
-    auto pin = [&](void **p, size_t bytes) { return cudaHostAlloc(p, bytes, cudaHostAllocDefault) == cudaSuccess; };
-    if (!pin((void **)&sv->hq, cap * sv->d * 4) || !pin((void **)&sv->hids, cap * kmax * 4) ||
-        !pin((void **)&sv->hdis, cap * kmax * 4) || !pin((void **)&sv->hk, cap * 4) || !pin((void **)&sv->hef, cap * 4) ||
-        !pin((void **)&sv->horder, cap * 4 * streams) || !pin((void **)&sv->hstatus, cap * 4))
-        return bad(fail(GSX_ERR_NOMEM, "pinned host allocation failed"));
-    sv->streams.resize(streams, nullptr);
-    sv->running.assign(streams, nullptr);
-    for (int i = 0; i < streams; ++i) sv->spill.emplace_back(new SpillTables);
-    for (auto &st : sv->streams) {
-        cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-        if (e != cudaSuccess) return bad(cuda_fail(e, "cudaStreamCreate"));
-    }
-    sv->ranges.init(sv->capacity);
-    sv->th = std::thread(dispatcher, sv);
-    *out = sv;
-    return GSX_OK;
+    try {
+        if (!s || !out) return fail(GSX_ERR_INVALID, "null argument");
+        if (!s->has_data) return fail(GSX_ERR_STATE, "server before set_data");
+        if (max_queries_in_flight <= 0 || kmax <= 0 || efmax <= 0 || streams <= 0 || streams > 32)
+            return fail(GSX_ERR_INVALID, "bad server arguments");
+        int rc;
+        GSX_CUDA(cudaSetDevice(s->device));
+        auto *sv = new gsx_server;
+        sv->s = s;
+        sv->kcap = kmax;
+        sv->efcap = efmax;
+        sv->nstreams = streams;
+        sv->d = s->ix.d;
+        // memory-based admission: the slot arena is sized so that it takes at most half of the free
+        // device memory
+        const size_t per_slot = (size_t)sv->d * 4 + (size_t)kmax * 8 + 16 + (size_t)streams * 4;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        size_t cap = (size_t)max_queries_in_flight;
+        if (per_slot * cap > free_b / 2) cap = std::max<size_t>(1, free_b / 2 / per_slot);
+        sv->capacity = (int)cap;
+        sv->max_group = std::max(256, sv->capacity / (2 * streams));
+        auto bad = [&](int code) {
+            gsx_server_destroy(sv);
+            return code;
+        };
+        if ((rc = sv->dq.ensure(cap * sv->d * 4)) || (rc = sv->dids.ensure(cap * kmax * 4)) ||
+            (rc = sv->ddis.ensure(cap * kmax * 4)) || (rc = sv->dk.ensure(cap * 4)) || (rc = sv->def.ensure(cap * 4)) ||
+            (rc = sv->dstatus.ensure(cap * 4)) || (rc = sv->dorder.ensure(cap * 4 * streams)) ||
+            (rc = sv->dcnt.ensure(64 * streams)))
+            return bad(rc);
+        auto pin = [&](void **p, size_t bytes) { return cudaHostAlloc(p, bytes, cudaHostAllocDefault) == cudaSuccess; };
+        if (!pin((void **)&sv->hq, cap * sv->d * 4) || !pin((void **)&sv->hids, cap * kmax * 4) ||
+            !pin((void **)&sv->hdis, cap * kmax * 4) || !pin((void **)&sv->hk, cap * 4) || !pin((void **)&sv->hef, cap * 4) ||
+            !pin((void **)&sv->horder, cap * 4 * streams) || !pin((void **)&sv->hstatus, cap * 4))
+            return bad(fail(GSX_ERR_NOMEM, "pinned host allocation failed"));
+        sv->streams.resize(streams, nullptr);
+        sv->running.assign(streams, nullptr);
+        for (int i = 0; i < streams; ++i) sv->spill.emplace_back(new SpillTables);
+        for (auto &st : sv->streams) {
+            cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            if (e != cudaSuccess) return bad(cuda_fail(e, "cudaStreamCreate"));
+        }
+        sv->ranges.init(sv->capacity);
+        sv->th = std::thread(dispatcher, sv);
+        *out = sv;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_server_create")
 }
 
 int gsx_server_capacity(const gsx_server *sv, int32_t *slots) {
-    if (!sv || !slots) return fail(GSX_ERR_INVALID, "null argument");
-    *slots = sv->capacity;
-    return GSX_OK;
+    try {
+        if (!sv || !slots) return fail(GSX_ERR_INVALID, "null argument");
+        *slots = sv->capacity;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_server_capacity")
 }
 
 int gsx_server_submit(gsx_server *sv, const float *queries, int32_t nq, int32_t k, int32_t ef, uint64_t *ticket) {
-    if (!sv || !queries || !ticket) return fail(GSX_ERR_INVALID, "null argument");
-    if (nq <= 0 || k <= 0 || ef <= 0) return fail(GSX_ERR_INVALID, "nq, k and ef must be positive");
-    if (k > sv->kcap || ef > sv->efcap) return fail(GSX_ERR_INVALID, "k or ef above the server's limits");
-    if (nq > sv->capacity) return fail(GSX_ERR_NOMEM, "request of %d queries exceeds the %d admitted slots", nq, sv->capacity);
-    auto *r = new Request;
-    r->nq = nq;
-    r->k = k;
-    r->ef = ef;
-    r->q.assign(queries, queries + (size_t)nq * sv->d);
-    r->ids.assign((size_t)nq * k, -1);
-    r->dis.assign((size_t)nq * k, 0.0f);
-    r->t_submit = Clock::now();
-    {
-        std::lock_guard<std::mutex> lk(sv->mu);
-        if (sv->stop) {
-            delete r;
-            return fail(GSX_ERR_STATE, "server is stopping");
+    try {
+        if (!sv || !queries || !ticket) return fail(GSX_ERR_INVALID, "null argument");
+        if (nq <= 0 || k <= 0 || ef <= 0) return fail(GSX_ERR_INVALID, "nq, k and ef must be positive");
+        if (k > sv->kcap || ef > sv->efcap) return fail(GSX_ERR_INVALID, "k or ef above the server's limits");
+        if (nq > sv->capacity) return fail(GSX_ERR_NOMEM, "request of %d queries exceeds the %d admitted slots", nq, sv->capacity);
+        auto *r = new Request;
+        r->nq = nq;
+        r->k = k;
+        r->ef = ef;
+        r->q.assign(queries, queries + (size_t)nq * sv->d);
+        r->ids.assign((size_t)nq * k, -1);
+        r->dis.assign((size_t)nq * k, 0.0f);
+        r->t_submit = Clock::now();
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            if (sv->stop) {
+                delete r;
+                return fail(GSX_ERR_STATE, "server is stopping");
+            }
+            r->ticket = sv->next_ticket++;
+            sv->reqs[r->ticket] = r;
+            sv->queue.push_back(r);
         }
-        r->ticket = sv->next_ticket++;
-        sv->reqs[r->ticket] = r;
-        sv->queue.push_back(r);
-    }
-    sv->cv.notify_one();
-    *ticket = r->ticket;
-    return GSX_OK;
+        sv->cv.notify_one();
+        *ticket = r->ticket;
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_server_submit")
 }
 
 int gsx_server_wait(gsx_server *sv, uint64_t ticket, int32_t timeout_ms, int32_t *ids, float *dis, double *latency_ms) {
-    if (!sv) return fail(GSX_ERR_INVALID, "null server");
-    std::unique_lock<std::mutex> lk(sv->mu);
-    auto it = sv->reqs.find(ticket);
-    if (it == sv->reqs.end()) return fail(GSX_ERR_INVALID, "unknown ticket %llu", (unsigned long long)ticket);
-    Request *r = it->second;
-    const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
-    while (r->state < 2) {
-        if (sv->done_cv.wait_until(lk, deadline) == std::cv_status::timeout && r->state < 2)
-            return fail(GSX_ERR_TIMEOUT, "request %llu not finished within %d ms", (unsigned long long)ticket, timeout_ms);
-    }
-    sv->reqs.erase(it);
-    lk.unlock();
-    std::unique_ptr<Request> own(r);
-    if (r->state == 3) return fail(r->err, "%s", r->msg.c_str());
-    if (ids) std::memcpy(ids, r->ids.data(), r->ids.size() * 4);
-    if (dis) std::memcpy(dis, r->dis.data(), r->dis.size() * 4);
-    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
-    return GSX_OK;
+    try {
+        if (!sv) return fail(GSX_ERR_INVALID, "null server");
+        std::unique_lock<std::mutex> lk(sv->mu);
+        auto it = sv->reqs.find(ticket);
+        if (it == sv->reqs.end()) return fail(GSX_ERR_INVALID, "unknown ticket %llu", (unsigned long long)ticket);
+        Request *r = it->second;
+        const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
+        while (r->state < 2) {
+            if (sv->done_cv.wait_until(lk, deadline) == std::cv_status::timeout && r->state < 2)
+                return fail(GSX_ERR_TIMEOUT, "request %llu not finished within %d ms", (unsigned long long)ticket, timeout_ms);
+        }
+        sv->reqs.erase(it);
+        lk.unlock();
+        std::unique_ptr<Request> own(r);
+        if (r->state == 3) return fail(r->err, "%s", r->msg.c_str());
+        if (ids) std::memcpy(ids, r->ids.data(), r->ids.size() * 4);
+        if (dis) std::memcpy(dis, r->dis.data(), r->dis.size() * 4);
+        if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_server_wait")
 }
 
 int gsx_server_stats(gsx_server *sv, int64_t *completed_queries, int32_t *queued_requests, int32_t *running_groups) {
-    if (!sv) return fail(GSX_ERR_INVALID, "null server");
-    std::lock_guard<std::mutex> lk(sv->mu);
-    if (completed_queries) *completed_queries = sv->completed_queries;
-    if (queued_requests) *queued_requests = (int32_t)sv->queue.size();
-    if (running_groups) {
-        int n = 0;
-        for (Group *g : sv->running) n += g != nullptr;
-        *running_groups = n;
-    }
-    return GSX_OK;
+    try {
+        if (!sv) return fail(GSX_ERR_INVALID, "null server");
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (completed_queries) *completed_queries = sv->completed_queries;
+        if (queued_requests) *queued_requests = (int32_t)sv->queue.size();
+        if (running_groups) {
+            int n = 0;
+            for (Group *g : sv->running) n += g != nullptr;
+            *running_groups = n;
+        }
+        return GSX_OK;
+    } GSX_ABI_GUARD("gsx_server_stats")
 }
 
 int gsx_server_drive_poisson(gsx_server *sv, const float *queries, int32_t nq_pool, int32_t n_requests,
                              double request_rate, int32_t size_min, int32_t size_max, const int32_t *ks, int32_t nk,
                              const int32_t *efs, int32_t nef, uint64_t seed, double *latency_ms, int32_t *sizes,
                              double *wall_s) {
-    if (!sv || !queries || !ks || !efs || !latency_ms || nk <= 0 || nef <= 0 || n_requests <= 0 || request_rate <= 0 ||
-        size_min <= 0 || size_max < size_min || size_max > nq_pool || size_max > sv->capacity)
-        return fail(GSX_ERR_INVALID, "bad load-driver arguments");
-    const int d = sv->d;
-    std::mt19937_64 rng(seed);
-    std::exponential_distribution<double> gap(request_rate);
-    std::uniform_real_distribution<double> u01(0.0, 1.0);
-    std::vector<double> at(n_requests);
-    std::vector<int32_t> sz(n_requests), kk(n_requests), ee(n_requests), off(n_requests);
-    double t = 0.0;
-    int64_t pos = 0;
-    const double lmin = std::log((double)size_min), lmax = std::log((double)size_max + 1.0);
-    for (int i = 0; i < n_requests; ++i) {
-        t += gap(rng);
-        at[i] = t;
-        sz[i] = std::min(size_max, (int32_t)std::floor(std::exp(lmin + (lmax - lmin) * u01(rng))));
-        kk[i] = ks[rng() % (uint64_t)nk];
-        ee[i] = efs[rng() % (uint64_t)nef];
-        if (pos + sz[i] > nq_pool) pos = 0;
-        off[i] = (int32_t)pos;
-        pos += sz[i];
-    }
-    std::vector<uint64_t> tickets(n_requests, 0);
-    std::atomic<int> submitted{0};
-    std::atomic<int> err{GSX_OK};
-    const auto t0 = Clock::now();
-    std::thread producer([&] {
+    try {
+        if (!sv || !queries || !ks || !efs || !latency_ms || nk <= 0 || nef <= 0 || n_requests <= 0 || request_rate <= 0 ||
+            size_min <= 0 || size_max < size_min || size_max > nq_pool || size_max > sv->capacity)
+            return fail(GSX_ERR_INVALID, "bad load-driver arguments");
+        const int d = sv->d;
+        std::mt19937_64 rng(seed);
+        std::exponential_distribution<double> gap(request_rate);
+        std::uniform_real_distribution<double> u01(0.0, 1.0);
+        std::vector<double> at(n_requests);
+        std::vector<int32_t> sz(n_requests), kk(n_requests), ee(n_requests), off(n_requests);
+        double t = 0.0;
+        int64_t pos = 0;
+        const double lmin = std::log((double)size_min), lmax = std::log((double)size_max + 1.0);
         for (int i = 0; i < n_requests; ++i) {
-            const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(at[i]));
-            // sleep most of the gap, then spin (bounded by the due time) for sub-millisecond precision
-            if (due - Clock::now() > std::chrono::microseconds(200))
-                std::this_thread::sleep_until(due - std::chrono::microseconds(100));
-            while (Clock::now() < due) {
+            t += gap(rng);
+            at[i] = t;
+            sz[i] = std::min(size_max, (int32_t)std::floor(std::exp(lmin + (lmax - lmin) * u01(rng))));
+            kk[i] = ks[rng() % (uint64_t)nk];
+            ee[i] = efs[rng() % (uint64_t)nef];
+            if (pos + sz[i] > nq_pool) pos = 0;
+            off[i] = (int32_t)pos;
+            pos += sz[i];
+        }
+        std::vector<uint64_t> tickets(n_requests, 0);
+        std::atomic<int> submitted{0};
+        std::atomic<int> err{GSX_OK};
+        const auto t0 = Clock::now();
+        std::thread producer([&] {
+            for (int i = 0; i < n_requests; ++i) {
+                const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(at[i]));
+                // sleep most of the gap, then spin (bounded by the due time) for sub-millisecond precision
+                if (due - Clock::now() > std::chrono::microseconds(200))
+                    std::this_thread::sleep_until(due - std::chrono::microseconds(100));
+                while (Clock::now() < due) {
+                }
+                uint64_t tk = 0;
+                const int rc = gsx_server_submit(sv, queries + (size_t)off[i] * d, sz[i], kk[i], ee[i], &tk);
+                if (rc != GSX_OK) {
+                    err.store(rc);
+                    break;
+                }
+                tickets[i] = tk;
+                submitted.store(i + 1, std::memory_order_release);
             }
-            uint64_t tk = 0;
-            const int rc = gsx_server_submit(sv, queries + (size_t)off[i] * d, sz[i], kk[i], ee[i], &tk);
-            if (rc != GSX_OK) {
-                err.store(rc);
+        });
+        int rc = GSX_OK;
+        for (int i = 0; i < n_requests && rc == GSX_OK; ++i) {
+            while (submitted.load(std::memory_order_acquire) <= i) {
+                if (err.load() != GSX_OK) break;
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+            }
+            if (err.load() != GSX_OK) {
+                rc = err.load();
                 break;
             }
-            tickets[i] = tk;
-            submitted.store(i + 1, std::memory_order_release);
+            rc = gsx_server_wait(sv, tickets[i], 120000, nullptr, nullptr, &latency_ms[i]);
+            if (sizes) sizes[i] = sz[i];
         }
-    });
-    int rc = GSX_OK;
-    for (int i = 0; i < n_requests && rc == GSX_OK; ++i) {
-        while (submitted.load(std::memory_order_acquire) <= i) {
-            if (err.load() != GSX_OK) break;
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
-        }
-        if (err.load() != GSX_OK) {
-            rc = err.load();
-            break;
-        }
-        rc = gsx_server_wait(sv, tickets[i], 120000, nullptr, nullptr, &latency_ms[i]);
-        if (sizes) sizes[i] = sz[i];
-    }
-    producer.join();
-    if (wall_s) *wall_s = std::chrono::duration<double>(Clock::now() - t0).count();
-    if (rc == GSX_OK && err.load() != GSX_OK) rc = err.load();
-    return rc;
+        producer.join();
+        if (wall_s) *wall_s = std::chrono::duration<double>(Clock::now() - t0).count();
+        if (rc == GSX_OK && err.load() != GSX_OK) rc = err.load();
+        return rc;
+    } GSX_ABI_GUARD("gsx_server_drive_poisson")
 }
 
 void gsx_server_destroy(gsx_server *sv) {

@@ -699,8 +699,10 @@ int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries
 
 extern "C" int gsx_knn_exact(const float *d_base, int64_t N, int32_t d, const float *d_queries, int32_t nq, int32_t k,
                              int32_t ip, int32_t *d_ids, float *d_dis, int32_t *exact_inputs, void *stream) {
-    if (!d_dis) return fail(GSX_ERR_INVALID, "bad arguments");
-    if (k > kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", kCand);
-    return knn_select(d_base, N, d, d_queries, nq, k, ip, 1, -1, 0, d_ids, d_dis, exact_inputs, nullptr,
-                      (cudaStream_t)stream);
+    try {
+        if (!d_dis) return fail(GSX_ERR_INVALID, "bad arguments");
+        if (k > kCand) return fail(GSX_ERR_INVALID, "k must be in [1, %d]", kCand);
+        return knn_select(d_base, N, d, d_queries, nq, k, ip, 1, -1, 0, d_ids, d_dis, exact_inputs, nullptr,
+                          (cudaStream_t)stream);
+    } GSX_ABI_GUARD("gsx_knn_exact")
 }
