@@ -543,7 +543,10 @@ __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState 
 template <int KIND, int METRIC, int LPR>
 __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpLayout &L, WarpState &w, int qi,
                            int lane) {
-    const int kq = bv.k_per ? bv.k_per[qi] : bv.k;
+    // a per-query k outside [0, out_stride] (a caller error on the device entry points) is clamped,
+    // so that no write leaves the query's output row
+    int kq = bv.k_per ? bv.k_per[qi] : bv.k;
+    kq = kq < 0 ? 0 : (kq > bv.out_stride ? bv.out_stride : kq);
     const int efq = bv.ef_per ? bv.ef_per[qi] : bv.ef;
     // Refiner: reorder_k = (int)(k * factor) (refiner.hpp:46, 73)
     const int rk = ix.has_refine ? (int)((float)kq * ix.refine_factor) : kq;
