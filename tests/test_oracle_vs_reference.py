@@ -247,3 +247,30 @@ def test_large_pools_match_the_reference(oracle, ref, quant, metric, refine):
         np.testing.assert_array_equal(ri, oi, err_msg=f"ef={ef} k={k}")
         np.testing.assert_array_equal(rd, od, err_msg=f"ef={ef} k={k}")
         assert rs.get_last_search_dist_cmps() == os_.get_last_search_dist_cmps()
+
+
+def test_mixed_ef_and_k_match_the_reference(oracle, ref):
+    """Per-query ef and k in one batch (the batched form the GPU takes, e.g. ef in {8..64}, k in
+    {1, 10, 25}): each query's result equals the reference's SearchBatch run with that query's ef
+    and k, since the reference has a single ef per call."""
+    from tests.golden import spec
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    p = os.path.join(root, "tests", "golden", "hnsw_d100.glass")
+    base, q = spec.base(), spec.queries()
+    rng = np.random.default_rng(3)
+    ef = rng.choice([8, 16, 32, 64], size=q.shape[0]).astype(np.int32)
+    k = rng.choice([1, 10, 25], size=q.shape[0]).astype(np.int32)
+    os_ = oracle.Searcher(oracle.Graph(p), base, "L2", "SQ4U", "FP32")
+    oi, od = os_.batch_search(q, int(k.max()), ef_per_query=ef, k_per_query=k)
+    rs = ref.Searcher(p, base, "L2", "SQ4U", "FP32")
+    for e in np.unique(ef):
+        for kk in np.unique(k):
+            sel = np.where((ef == e) & (k == kk))[0]
+            if sel.size == 0:
+                continue
+            rs.set_ef(int(e))
+            ri, rd = rs.batch_search(q[sel], int(kk))
+            np.testing.assert_array_equal(oi[sel, :kk], ri, err_msg=f"ef={e} k={kk}")
+            np.testing.assert_array_equal(od[sel, :kk], rd, err_msg=f"ef={e} k={kk}")
+            assert (oi[sel, kk:] == -1).all()
