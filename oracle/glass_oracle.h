@@ -96,9 +96,12 @@ void go_search(const go_index *ix, const float *queries, int64_t nq, int k, int 
 
 /* NSG / SSG graph build (oracle/nsg_oracle.c).  knng_in (may be NULL: computed) is N x min(knn_k,
  * N - 1); ep_in < 0 computes the entry point.  Writes knng_out (same shape), graph_out (N x R, -1
- * padded), the entry point and the number of nodes attached for connectivity.  0 on success. */
+ * padded), the entry point and the number of nodes attached for connectivity, and, when link_out is
+ * not NULL, the pruned forward graph of the link step before reverse links (N x R, -1 padded).
+ * 0 on success. */
 int go_nsg_build(const float *x, int64_t N, int d, int R, int L, int ssg, int knn_k, const int32_t *knng_in,
-                 int32_t ep_in, int32_t *knng_out, int32_t *graph_out, int32_t *ep_out, int32_t *n_attached);
+                 int32_t ep_in, int32_t *knng_out, int32_t *graph_out, int32_t *ep_out, int32_t *n_attached,
+                 int32_t *link_out);
 
 #ifdef __cplusplus
 }

@@ -127,7 +127,8 @@ static int occluded(const float *x, int d, const int32_t *rid, const float *rd, 
 }
 
 int go_nsg_build(const float *x, int64_t N, int d, int R, int L, int ssg, int knn_k, const int32_t *knng_in,
-                 int32_t ep_in, int32_t *knng_out, int32_t *graph_out, int32_t *ep_out, int32_t *n_attached) {
+                 int32_t ep_in, int32_t *knng_out, int32_t *graph_out, int32_t *ep_out, int32_t *n_attached,
+                 int32_t *link_out) {
     if (N < 2 || d <= 0 || R <= 0 || knn_k <= 0) return 1;
     if (L == 0) L = R + 32;
     const int C = R + 100;
@@ -310,6 +311,7 @@ int go_nsg_build(const float *x, int64_t N, int d, int R, int L, int ssg, int kn
     free(off);
     free(fill);
     free(offers);
+    if (link_out) memcpy(link_out, lid, sizeof(int32_t) * (size_t)N * R);
     free(lid);
     free(ldis);
     /* connectivity (nsg.hpp:317-404) */

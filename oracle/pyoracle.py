@@ -86,7 +86,8 @@ def _oracle_lib():
         lib.go_search.argtypes = [C.POINTER(_GoIndex), _f32p, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                   C.c_int, _i32p, _f32p, _i64p, C.c_int]
         lib.go_nsg_build.argtypes = [_f32p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
-                                     C.c_int32, _i32p, _i32p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+                                     C.c_int32, _i32p, _i32p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                     C.c_void_p]
         lib.go_nsg_build.restype = C.c_int
         _lib = lib
     return _lib
@@ -208,9 +209,11 @@ class Searcher:
         return float(self.last_cmps.mean()) if self.last_cmps is not None else 0.0
 
 
-def nsg_build(data: np.ndarray, R: int, L: int = 0, ssg: bool = False, knn_k: int = 64, knng=None, ep: int = -1):
+def nsg_build(data: np.ndarray, R: int, L: int = 0, ssg: bool = False, knn_k: int = 64, knng=None, ep: int = -1,
+              return_link: bool = False):
     """The restated NSG / SSG build (oracle/nsg_oracle.c): returns (graph N x R, entry point, kNN
-    graph, nodes attached by the connectivity pass).  knng / ep, when given, replace the oracle's own
+    graph, nodes attached by the connectivity pass), plus the pruned forward graph of the link step
+    (before reverse links) when return_link is set.  knng / ep, when given, replace the oracle's own
     kNN graph / entry point."""
     data = np.ascontiguousarray(data, dtype=np.float32)
     n, d = data.shape
@@ -222,11 +225,14 @@ def nsg_build(data: np.ndarray, R: int, L: int = 0, ssg: bool = False, knn_k: in
         assert kin.shape == (n, k)
     g = np.zeros((n, R), np.int32)
     ep_out, att = C.c_int32(), C.c_int32()
+    link = np.zeros((n, R), np.int32) if return_link else None
     rc = _oracle_lib().go_nsg_build(data, n, d, R, L, 1 if ssg else 0, knn_k,
                                     kin.ctypes.data if kin is not None else None, int(ep), kn, g,
-                                    C.byref(ep_out), C.byref(att))
+                                    C.byref(ep_out), C.byref(att), link.ctypes.data if return_link else None)
     if rc != 0:
         raise RuntimeError(f"oracle NSG build failed ({rc})")
+    if return_link:
+        return g, ep_out.value, kn, att.value, link
     return g, ep_out.value, kn, att.value
 
 
@@ -251,6 +257,9 @@ def _ref_lib():
         lib.ref_searcher_dist_cmps.argtypes = [C.c_void_p]
         lib.ref_searcher_dist_cmps.restype = C.c_double
         lib.ref_searcher_destroy.argtypes = [C.c_void_p]
+        lib.ref_nsg_link.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i32p, C.c_int, C.c_int,
+                                     _i32p]
+        lib.ref_nsg_link.restype = C.c_int
         lib.ref_graph_open.argtypes = [C.c_char_p, C.c_char_p]
         lib.ref_graph_open.restype = C.c_void_p
         lib.ref_graph_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -276,6 +285,19 @@ class RefGlass:
         data = np.ascontiguousarray(data, dtype=np.float32)
         return _ref_lib().ref_build_graph(index_type.encode(), data, data.shape[0], data.shape[1], metric.encode(),
                                           quant.encode(), int(R), int(L), path.encode())
+
+    @staticmethod
+    def nsg_link(data, R, L, ssg, knng, ep):
+        """The reference NSG's per-node link step (search_on_graph + sync_prune) over a given kNN
+        graph and entry point, FP32 distances: the pruned forward graph, N x R, -1 padded."""
+        data = np.ascontiguousarray(data, dtype=np.float32)
+        knng = np.ascontiguousarray(knng, dtype=np.int32)
+        out = np.zeros((data.shape[0], R), np.int32)
+        rc = _ref_lib().ref_nsg_link(data, data.shape[0], data.shape[1], int(R), int(L), 1 if ssg else 0, knng,
+                                     knng.shape[1], int(ep), out)
+        if rc != 0:
+            raise RuntimeError("reference link step failed")
+        return out
 
     @staticmethod
     def load_graph(path, fmt="glass"):

@@ -137,6 +137,34 @@ double ref_searcher_dist_cmps(void *h) { return ((RefSearcher *)h)->s->GetLastSe
 
 void ref_searcher_destroy(void *h) { delete (RefSearcher *)h; }
 
+// The reference NSG's link step for every node (the first loop of NSG::link, nsg.hpp:166-176:
+// search_on_graph, then sync_prune) over a given kNN graph and entry point, with the FP32
+// quantizer's symmetric distances; writes the pruned forward graph (before add_reverse_links).
+int ref_nsg_link(const float *data, int n, int d, int R, int L, int ssg, const int *knng, int K, int ep, int *out) {
+    using Q = glass::FP32Quantizer<glass::Metric::L2>;
+    glass::NSG<Q> nsg(R, L, ssg != 0);
+    nsg.nb = n;
+    nsg.d = d;
+    nsg.ep = ep;
+    Q quant(d);
+    quant.train(data, n);
+    quant.add(data, n);
+    auto computer = quant.get_sym_computer();
+    glass::Graph<int> kg(n, K);
+    std::memcpy(kg.data, knng, (size_t)n * K * 4);
+    glass::Graph<glass::Node> tmp(n, R);
+#pragma omp parallel for schedule(dynamic)
+    for (int i = 0; i < n; ++i) {
+        std::vector<glass::Node> fullset;
+        glass::LinearPool<float> pool(n, nsg.L, nsg.L);
+        nsg.search_on_graph(computer, i, kg, ep, pool, fullset);
+        nsg.sync_prune(computer, i, pool, fullset, kg, tmp);
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < R; ++j) out[(size_t)i * R + j] = tmp.at(i, j).id;
+    return 0;
+}
+
 // A graph read by the reference's own loader (Graph<int>::load, glass/graph.hpp:121-135, with its
 // glass / diskann / hnswlib / nsg readers), for comparison with the product's loaders.
 void *ref_graph_open(const char *path, const char *format) {
