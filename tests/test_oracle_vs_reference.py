@@ -276,17 +276,18 @@ def test_mixed_ef_and_k_match_the_reference(oracle, ref):
             assert (oi[sel, kk:] == -1).all()
 
 
+@pytest.mark.parametrize("ssg", [False, True])
 @pytest.mark.parametrize("n,d,R,L", [(1500, 32, 16, 40), (3000, 64, 24, 0), (800, 7, 8, 24)])
-def test_nsg_link_step_matches_the_reference(oracle, ref, n, d, R, L):
+def test_nsg_link_step_matches_the_reference(oracle, ref, n, d, R, L, ssg):
     """The link step of the NSG build (per node: search_on_graph over the kNN graph from the entry
-    point, then sync_prune with the NSG rule; nsg.hpp:129-246) run by the oracle and by the
+    point, then sync_prune with the NSG or the SSG rule; nsg.hpp:129-246) run by the oracle and by the
     reference's own NSG code on the same kNN graph and entry point gives the same pruned forward
     graph.  Integer-valued rows keep every squared distance exact in fp32, so the reference's
     AVX-512 sums and the oracle's equal bit for bit.  (The kNN graph itself is NN-Descent in the
     reference, random; the reverse-link and connectivity passes depend on thread timing and random
     draws there.  The GPU build equals the oracle in every stage.)"""
     x = datasets.cluster_mixture(n, d=d, n_clusters=24, seed=31)
-    g, ep, knng, _, link = oracle.nsg_build(x, R, L, return_link=True)
-    want = ref.nsg_link(x, R, L, False, knng, ep)
+    g, ep, knng, _, link = oracle.nsg_build(x, R, L, ssg=ssg, return_link=True)
+    want = ref.nsg_link(x, R, L, ssg, knng, ep)
     np.testing.assert_array_equal(link, want)
     assert (link[:, 0] >= 0).all()
