@@ -260,6 +260,8 @@ def _ref_lib():
         lib.ref_nsg_link.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i32p, C.c_int, C.c_int,
                                      _i32p]
         lib.ref_nsg_link.restype = C.c_int
+        lib.ref_nsg_init.argtypes = [_f32p, C.c_int, C.c_int]
+        lib.ref_nsg_init.restype = C.c_int
         lib.ref_graph_open.argtypes = [C.c_char_p, C.c_char_p]
         lib.ref_graph_open.restype = C.c_void_p
         lib.ref_graph_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -298,6 +300,12 @@ class RefGlass:
         if rc != 0:
             raise RuntimeError("reference link step failed")
         return out
+
+    @staticmethod
+    def nsg_entry_point(data):
+        """The reference NSG's entry point: the row nearest the centroid (NSG::Init)."""
+        data = np.ascontiguousarray(data, dtype=np.float32)
+        return int(_ref_lib().ref_nsg_init(data, data.shape[0], data.shape[1]))
 
     @staticmethod
     def load_graph(path, fmt="glass"):

@@ -165,6 +165,20 @@ int ref_nsg_link(const float *data, int n, int d, int R, int L, int ssg, const i
     return 0;
 }
 
+// The reference NSG's entry point (NSG::Init, nsg.hpp:106-127: the row nearest the float centroid
+// by the FP32 quantizer's distance).
+int ref_nsg_init(const float *data, int n, int d) {
+    using Q = glass::FP32Quantizer<glass::Metric::L2>;
+    glass::NSG<Q> nsg(32, 0, false);
+    nsg.nb = n;
+    nsg.d = d;
+    Q quant(d);
+    quant.train(data, n);
+    quant.add(data, n);
+    nsg.Init(quant, data);
+    return nsg.ep;
+}
+
 // A graph read by the reference's own loader (Graph<int>::load, glass/graph.hpp:121-135, with its
 // glass / diskann / hnswlib / nsg readers), for comparison with the product's loaders.
 void *ref_graph_open(const char *path, const char *format) {

@@ -291,3 +291,15 @@ def test_nsg_link_step_matches_the_reference(oracle, ref, n, d, R, L, ssg):
     want = ref.nsg_link(x, R, L, ssg, knng, ep)
     np.testing.assert_array_equal(link, want)
     assert (link[:, 0] >= 0).all()
+
+
+@pytest.mark.parametrize("n,d,seed", [(1500, 32, 31), (800, 7, 31), (20000, 128, 2), (5000, 100, 7)])
+def test_nsg_entry_point_matches_the_reference(oracle, ref, n, d, seed):
+    """The build's entry point (the row nearest the centroid, NSG::Init, nsg.hpp:106-127): the
+    oracle's equals the reference's on integer rows (exact centroid sums) and on float rows."""
+    # a ring stands in for the kNN graph: only the entry point is compared
+    ring = np.stack([(np.arange(n) + 1) % n, (np.arange(n) + 2) % n], axis=1).astype(np.int32)
+    x = datasets.cluster_mixture(n, d=d, n_clusters=24, seed=seed)
+    assert oracle.nsg_build(x, 16, 40, knn_k=2, knng=ring)[1] == ref.nsg_entry_point(x)
+    y = datasets.gaussian(n, d, seed=seed)
+    assert oracle.nsg_build(y, 16, 40, knn_k=2, knng=ring)[1] == ref.nsg_entry_point(y)
