@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <new>
 
 #include "gsx_host.h"
@@ -140,7 +141,7 @@ extern "C" int gsx_searcher_capture_batch(gsx_searcher *s, const float *d_querie
         if (kmax < k) kmax = k;
         cudaError_t e = cudaSetDevice(s->device);
         if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
-        gsx_batch_graph *g = new (std::nothrow) gsx_batch_graph;
+        std::unique_ptr<gsx_batch_graph> g(new (std::nothrow) gsx_batch_graph);
         if (!g) return fail(GSX_ERR_NOMEM, "out of host memory");
         g->s = s;
         g->device = s->device;
@@ -155,12 +156,9 @@ extern "C" int gsx_searcher_capture_batch(gsx_searcher *s, const float *d_querie
         g->dis = d_dis;
         g->cmps = d_cmps;
         g->exps = d_expansions;
-        const int rc = make_graph(g);
-        if (rc) {
-            delete g;
-            return rc;
-        }
-        *out = g;
+        const int rc = make_graph(g.get());
+        if (rc) return rc;  // the graph object and its scratch are freed here
+        *out = g.release();
         return GSX_OK;
     } GSX_ABI_GUARD("gsx_searcher_capture_batch")
 }
