@@ -103,3 +103,61 @@ def test_random_case(oracle, ref, tmp_path, case):
         for i in range(2):
             a, b = rs.search(q[i], k), os_.search(q[i], k)
             check(a[0][None], a[1][None], b[0][None], b[1][None], os_.last_cmps, k, f"single ef={ef} k={k}")
+
+
+def random_hnsw(rng, n):
+    """Random HNSW upper levels in the glass layout (HNSWInitializer.hpp:64-86): geometric levels,
+    each list of hK ids drawn among the nodes present on that level, cut short by -1; the entry point
+    is a node of the top level."""
+    hK = int(rng.integers(1, 17))
+    levels = np.minimum(rng.geometric(0.5, size=n) - 1, 5)
+    top = int(levels.max())
+    ep = int(rng.choice(np.where(levels == top)[0]))
+    by_level = {lv: np.where(levels >= lv)[0] for lv in range(1, top + 1)}
+    lists = []
+    for u in range(n):
+        flat = []
+        for lv in range(1, int(levels[u]) + 1):
+            cand = by_level[lv]
+            row = list(rng.choice(cand, size=hK).astype(int))
+            cut = int(rng.integers(0, hK + 1))
+            row = row[:cut] + [-1] * (hK - cut)
+            flat += row
+        lists.append(np.array(flat, np.int32))
+    return hK, ep, lists
+
+
+@pytest.mark.parametrize("case", range(30))
+def test_random_hnsw_case(oracle, ref, tmp_path, case):
+    """Random graphs with random HNSW upper levels: the greedy descent (HNSWInitializer::initialize)
+    and the search after it, oracle against reference."""
+    rng = np.random.default_rng(5000 + case)
+    n = int(rng.integers(50, 1200))
+    d = int(rng.integers(1, 100))
+    quant, metric, refine = [c for c in spec.SEARCHERS if not c[2]][int(rng.integers(0, 13))]
+    x = rng.standard_normal((n, d)).astype(np.float32)
+    q = rng.standard_normal((15, d)).astype(np.float32)
+    adj, _ = random_graph(rng, n)
+    hnsw = random_hnsw(rng, n)
+    p = str(tmp_path / "h.glass")
+    write_glass(p, adj, [hnsw[1]], hnsw=hnsw)
+    xz = np.zeros((n + 16 // d + 1, d), np.float32)
+    xz[:n] = x
+    rs = ref.Searcher(p, xz[:n], metric, quant, refine)
+    os_ = oracle.Searcher(oracle.Graph(p), x, metric, quant, refine)
+    tol = (quant, metric) == ("SQ8", "L2")
+    for ef, k in [(int(rng.integers(1, 200)), int(rng.integers(1, 50))), (1, 1)]:
+        rs.set_ef(ef)
+        os_.set_ef(ef)
+        ri, rd = rs.batch_search(q, k)
+        oi, od = os_.batch_search(q, k)
+        for i in range(q.shape[0]):
+            # the upper-level descent's distances count but do not enter the pool, so the pool size is
+            # read from the oracle's output: its entries past the pool are -1 (the reference's stale)
+            m = int((oi[i] >= 0).sum())
+            np.testing.assert_array_equal(ri[i, :m], oi[i, :m], err_msg=f"case {case} {quant}/{metric} ef={ef} k={k}")
+            if tol:
+                np.testing.assert_allclose(rd[i, :m], od[i, :m], rtol=1e-5, atol=0)
+            else:
+                np.testing.assert_array_equal(rd[i, :m], od[i, :m], err_msg=f"case {case} ef={ef} k={k}")
+        assert rs.get_last_search_dist_cmps() == os_.get_last_search_dist_cmps()
