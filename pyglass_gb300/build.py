@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["search_kernel.cu", "encode_kernel.cu", "order_kernel.cu", "calib_kernel.cu", "noalloc.cu", "knn_kernel.cu",
                 "build_kernel.cu"]
 HOST_SOURCES = ["gsx_api.cpp", "gsx_graph.cpp", "gsx_server.cpp", "gsx_capture.cpp"]
-HEADERS = ["gsx_internal.h", "gsx_device.cuh", "gsx_host.h"]
+HEADERS = ["gsx_internal.h", "gsx_device.cuh", "gsx_host.h", "gsx_ranges.h"]
 
 
 def _newer(out: str, deps: list[str]) -> bool:
