@@ -1,0 +1,43 @@
+"""Host-side pieces of bench.py that shape its JSON line, checked without a GPU: the clock summary
+(median SM clock under load, throttle reasons seen inside the timed region only) and the graph
+fallback's bookkeeping."""
+
+import bench
+
+
+def _row(sm, mx, **active):
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    flags = ["Active" if active.get(n) else "Not Active" for n in names]
+    return ["0", str(sm), str(mx), "900.0", "0x0", *flags]
+
+
+def test_clock_summary_uses_the_timed_region_only():
+    c = bench.Clocks(0)
+    c.t0, c.t1 = 10.0, 20.0
+    c.rows = [(9.0, _row(500, 2070, hw_thermal_slowdown=True)),  # before the region: ignored
+              (11.0, _row(2000, 2070)), (12.0, _row(2070, 2070, sw_power_cap=True)), (13.0, _row(1900, 2070)),
+              (25.0, _row(600, 2070, hw_slowdown=True))]  # after the region: ignored
+    s = c.summary()
+    assert s["sm_mhz"] == 2000.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    assert s["samples"] == 3
+
+
+def test_clock_summary_without_samples():
+    c = bench.Clocks(0)
+    c.t0, c.t1 = 1.0, 2.0
+    assert c.summary()["reasons"] == ["unsampled"]
+
+
+def test_graph_source_names_the_fallback():
+    saved = dict(bench._BUILT)
+    try:
+        bench._BUILT.clear()
+        assert "reference's CPU builder" in bench.graph_source()
+        bench._BUILT.update(path="/tmp/x.glass", seconds=3.0)
+        assert "GPU builder" in bench.graph_source() and "absent" in bench.graph_source()
+        bench._BUILT["stale"] = True
+        assert "differ" in bench.graph_source()
+    finally:
+        bench._BUILT.clear()
+        bench._BUILT.update(saved)
