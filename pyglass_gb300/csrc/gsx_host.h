@@ -37,6 +37,23 @@ int cuda_fail(cudaError_t e, const char *what);
         if (e_ != cudaSuccess) return ::gsx::cuda_fail(e_, #call); \
     } while (0)
 
+// Makes `device` current for the scope and gives the caller's current device back on exit, so an
+// entry point leaves the calling thread's CUDA state as it found it.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != device) err = cudaSetDevice(device);
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
 struct HostGraph {
     int32_t N = 0, K = 0;
     std::vector<int32_t> adj;
