@@ -473,6 +473,40 @@ int go_graph_load(const char *path, go_graph *g) {
     return ok ? 0 : -2;
 }
 
+/* NSG-format graph (glass/graph.hpp:224-246, Graph::load_nsg): K, the entry point, then per node
+ * its neighbour count and ids; N is the number of node records the file holds and rows are padded
+ * with -1 to K.  A count outside [0, K] or a truncated record is an error here, where the
+ * reference would read past its row. */
+int go_graph_load_nsg(const char *path, go_graph *g) {
+    memset(g, 0, sizeof(*g));
+    FILE *f = fopen(path, "rb");
+    if (!f) return -1;
+    int32_t hdr[2];
+    if (fread(hdr, 4, 2, f) != 2 || hdr[0] <= 0) { fclose(f); return -2; }
+    g->K = hdr[0];
+    g->nep = 1;
+    g->eps = (int32_t *)malloc(sizeof(int32_t));
+    g->eps[0] = hdr[1];
+    size_t cap = 1 << 16, n = 0;
+    g->adj = (int32_t *)malloc(sizeof(int32_t) * cap * (size_t)g->K);
+    int32_t c;
+    while (fread(&c, 4, 1, f) == 1) {
+        if (c < 0 || c > g->K) { fclose(f); return -2; }
+        if (n == cap) {
+            cap *= 2;
+            g->adj = (int32_t *)realloc(g->adj, sizeof(int32_t) * cap * (size_t)g->K);
+        }
+        int32_t *row = g->adj + n * (size_t)g->K;
+        if (fread(row, 4, (size_t)c, f) != (size_t)c) { fclose(f); return -2; }
+        for (int32_t j = c; j < g->K; ++j) row[j] = -1;
+        ++n;
+    }
+    fclose(f);
+    if (n == 0 || n > 0x7fffffff) return -2;
+    g->N = (int32_t)n;
+    return 0;
+}
+
 void go_graph_free(go_graph *g) {
     free(g->adj); free(g->eps); free(g->levels); free(g->loff); free(g->lists);
     memset(g, 0, sizeof(*g));

@@ -66,6 +66,7 @@ typedef struct {
 } go_graph;
 
 int go_graph_load(const char *path, go_graph *g);
+int go_graph_load_nsg(const char *path, go_graph *g);
 void go_graph_free(go_graph *g);
 
 /* Encoded index: graph + codes of the search quantizer (+ optional FP32 refine store). */

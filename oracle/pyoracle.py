@@ -20,7 +20,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libglass_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libglass_ref.so")
-REFERENCE_DIR = os.environ.get("GLASS_REFERENCE_DIR", "/root/reference")
+
+
+def reference_dir() -> str | None:
+    """The pyglass checkout the reference driver is compiled from: the GLASS_REFERENCE_DIR
+    environment variable (the build entry point sets it on a host that has the checkout), or None."""
+    d = os.environ.get("GLASS_REFERENCE_DIR")
+    return d if d and os.path.isdir(os.path.join(d, "glass")) else None
 
 KIND = {"FP32": 0, "FP16": 1, "BF16": 2, "E5M2": 3, "SQ8U": 4, "SQ8": 5, "SQ4U": 7, "SQ4UA": 8, "SQ2U": 11, "SQ1": 12}
 METRIC = {"L2": 0, "IP": 1}
@@ -37,10 +43,13 @@ _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 def build(ref: bool | None = None) -> None:
     """Compiles the oracle (always) and the reference driver (when the reference is present)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    src = reference_dir()
     if ref is None:
-        ref = os.path.isdir(os.path.join(REFERENCE_DIR, "glass"))
+        ref = src is not None
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={REFERENCE_DIR}"], check=True)
+        if src is None:
+            raise RuntimeError("the reference driver needs GLASS_REFERENCE_DIR (a pyglass checkout)")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={src}"], check=True)
 
 
 def ref_available() -> bool:
@@ -82,6 +91,7 @@ def _oracle_lib():
         lib.go_query_distances.argtypes = [C.c_int, C.c_int, _f32p, C.c_int, _f32p, C.c_int64, _u8p, _i32p,
                                            C.c_int, _f64p]
         lib.go_graph_load.argtypes = [C.c_char_p, C.POINTER(_GoGraph)]
+        lib.go_graph_load_nsg.argtypes = [C.c_char_p, C.POINTER(_GoGraph)]
         lib.go_graph_free.argtypes = [C.POINTER(_GoGraph)]
         lib.go_search.argtypes = [C.POINTER(_GoIndex), _f32p, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                   C.c_int, _i32p, _f32p, _i64p, C.c_int]
@@ -133,11 +143,16 @@ class Quant:
 
 
 class Graph:
-    def __init__(self, path: str):
+    """A graph file in the glass format (with HNSW levels) or the NSG format."""
+
+    def __init__(self, path: str, fmt: str = "glass"):
         self._g = _GoGraph()
-        rc = _oracle_lib().go_graph_load(path.encode(), C.byref(self._g))
+        load = {"glass": _oracle_lib().go_graph_load, "nsg": _oracle_lib().go_graph_load_nsg}.get(fmt)
+        if load is None:
+            raise ValueError(f"the oracle reads glass and nsg graph files, not {fmt!r}")
+        rc = load(path.encode(), C.byref(self._g))
         if rc != 0:
-            raise IOError(f"cannot load glass graph {path} ({rc})")
+            raise IOError(f"cannot load {fmt} graph {path} ({rc})")
         self.N, self.K = self._g.N, self._g.K
 
     def adjacency(self) -> np.ndarray:

@@ -60,7 +60,11 @@ def low_rank(n: int, d: int = 960, rank: int = 32, noise: float = 0.05, seed: in
 
 def normalized_mixture(n: int, d: int = 768, n_clusters: int = 4096, sigma: float = 0.3, seed: int = 4,
                        stream: int = 0) -> np.ndarray:
-    """Unit-length rows of a Gaussian mixture (centers ~ N(0, I), within-cluster sigma)."""
+    """Unit-length rows of a Gaussian mixture (centers ~ N(0, I), within-cluster sigma).
+
+    The row norms are sums of float64 squares taken column by column in a fixed order, and every
+    other step is one correctly rounded elementwise operation, so x86 and aarch64 hosts produce the
+    same bytes (a float32 ``np.linalg.norm`` reduces in SIMD-width-dependent order and does not)."""
     centers = np.random.default_rng([seed, 999]).standard_normal((n_clusters, d), dtype=np.float32)
     rng = np.random.default_rng([seed, stream])
     out = np.empty((n, d), np.float32)
@@ -68,8 +72,11 @@ def normalized_mixture(n: int, d: int = 768, n_clusters: int = 4096, sigma: floa
         m = min(_CHUNK, n - s)
         lab = rng.integers(0, n_clusters, size=m)
         x = centers[lab] + rng.standard_normal((m, d), dtype=np.float32) * np.float32(sigma)
-        x /= np.linalg.norm(x, axis=1, keepdims=True)
-        out[s:s + m] = x
+        xt = np.ascontiguousarray(x.T).astype(np.float64)
+        ss = np.zeros(m)
+        for j in range(d):
+            ss += xt[j] * xt[j]
+        out[s:s + m] = (xt / np.sqrt(ss)).T.astype(np.float32)
     return out
 
 

@@ -14,6 +14,9 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def oracle():
+    import __graft_entry__
+
+    __graft_entry__.reference_env()
     from oracle import pyoracle
 
     pyoracle.build(ref=None)

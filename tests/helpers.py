@@ -44,9 +44,10 @@ def recall(ids, gt, k):
 
 
 def oracle_graph(oracle, glass, path, fmt):
-    """The oracle reads glass files only: other formats are converted through the library's loader."""
-    if fmt == "glass":
-        return oracle.Graph(path)
+    """The oracle reads glass and NSG files itself; other formats are converted through the library's
+    loader."""
+    if fmt in ("glass", "nsg"):
+        return oracle.Graph(path, fmt)
     import os
     import tempfile
 

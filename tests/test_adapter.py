@@ -44,8 +44,8 @@ int main() {
 
 @pytest.fixture(scope="module")
 def reference_dir(oracle, glass):
-    d = oracle.REFERENCE_DIR
-    if not os.path.exists(os.path.join(d, "glass", "searcher", "searcher_base.hpp")):
+    d = oracle.reference_dir()
+    if d is None or not os.path.exists(os.path.join(d, "glass", "searcher", "searcher_base.hpp")):
         pytest.skip("reference checkout not available on this host")
     return d
 

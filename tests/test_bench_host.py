@@ -41,3 +41,35 @@ def test_graph_source_names_the_fallback():
     finally:
         bench._BUILT.clear()
         bench._BUILT.update(saved)
+
+
+def test_cpu_legs_load_no_library_of_the_package(tmp_path):
+    """The reference arm and the CPU baseline search through the oracle's own graph readers, so the
+    process maps the oracle's library and none of this package's (checked in a child process on the
+    golden graph's NSG-format twin)."""
+    import os
+    import shutil
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "g.glass"
+    shutil.copy(os.path.join(root, "tests", "golden", "nsg_d100.glass"), src)
+    from oracle import compact_graphs
+
+    twin = compact_graphs.compact(str(src))
+    code = f"""
+import sys
+sys.path.insert(0, {root!r})
+import bench
+from tests.golden import spec
+bench.graph_file = lambda: ({twin!r}, "nsg")
+cb, s, ids = bench.cpu_baseline(spec.base(), spec.queries(), 32, 50)
+assert ids.shape == (50, 10) and (ids >= 0).all()
+maps = open("/proc/self/maps").read()
+assert "libglass_oracle.so" in maps
+assert "libglass_gb300" not in maps and "_glass" not in maps, "package library mapped"
+print("ok")
+"""
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stdout + r.stderr

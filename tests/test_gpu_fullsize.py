@@ -31,11 +31,12 @@ def test_clusters1m_sq4u_refine_matches_oracle(gpu, oracle, workload):
     base, q = workload
     s = gpu.Searcher(gpu.Graph(*FOUND), base, "L2", "SQ4U", "FP32")
     o = oracle.Searcher(oracle_graph(oracle, gpu, *FOUND), base, "L2", "SQ4U", "FP32")
-    for ef in (16, 64):
+    for ef in (16, 64, 128):
         s.set_ef(ef)
         o.set_ef(ef)
         gi, gd = s.batch_search(q, 10)
-        sample = np.arange(0, q.shape[0], 25)
+        # every 25th query, and at the benchmark's ef 128 all 10,000
+        sample = np.arange(0, q.shape[0], 1 if ef == 128 else 25)
         oi, od = o.batch_search(q[sample], 10)
         np.testing.assert_array_equal(gi[sample], oi)
         np.testing.assert_array_equal(gd[sample], od)

@@ -43,3 +43,21 @@ def test_search(oracle, golden, case):
         np.testing.assert_allclose(dis, golden[f"dis/{key}"], rtol=spec.RTOL, atol=0)
     else:
         np.testing.assert_array_equal(dis, golden[f"dis/{key}"])
+
+
+def test_nsg_reader_equals_glass_reader(oracle, tmp_path):
+    """The oracle's NSG-format reader (Graph::load_nsg, glass/graph.hpp:224-246) gives the graph the
+    glass reader gives for the same rows: the compact twin oracle/compact_graphs.py writes."""
+    import shutil
+
+    from oracle import compact_graphs
+
+    src = tmp_path / "g.glass"
+    shutil.copy(os.path.join(GOLDEN_DIR, "nsg_d100.glass"), src)
+    twin = compact_graphs.compact(str(src))
+    a, b = oracle.Graph(str(src)), oracle.Graph(twin, "nsg")
+    assert (a.N, a.K) == (b.N, b.K)
+    np.testing.assert_array_equal(a.adjacency(), b.adjacency())
+    assert a._g.eps[0] == b._g.eps[0]
+    with pytest.raises(ValueError):
+        oracle.Graph(twin, "diskann")
