@@ -147,9 +147,17 @@ int gsx_batch_graph_destroy(gsx_batch_graph *g);
  * contents: calls that overlap on the GPU (other streams or threads) race, so the caller must
  * serialise them.  Enqueued on `stream` (NULL = the searcher's stream) with the searcher's ef,
  * without synchronising.  A query whose visited set outgrows its shared-memory table is left
- * unanswered (all its k ids are -1); the allocating entry points answer every query. */
+ * unanswered: all its k ids are -1 and its distances +inf (the allocating entry points answer every
+ * query).  A query that ran to the end always returns at least one id, since its entry point enters
+ * its pool, so ids[q*k] == -1 marks an unanswered query; gsx_searcher_noalloc_overflow_count gives
+ * how many there were.  The current CUDA device of the calling thread is unchanged on return. */
 int gsx_searcher_search_batch_noalloc(gsx_searcher *s, const float *d_queries, int32_t nq, int32_t k,
                                       int32_t *d_ids, float *d_dis, void *stream);
+/* Number of queries the latest allocation-free search on the searcher's device left unanswered,
+ * read from the same fixed array (no allocation).  Call it after synchronising the stream that
+ * search ran on; it reads whatever the array holds at that moment, so a later allocation-free call
+ * on the device replaces the count.  No counterpart in the reference. */
+int gsx_searcher_noalloc_overflow_count(gsx_searcher *s, uint32_t *count);
 
 /* Same as above with HOST buffers (copies inside), synchronous. */
 int gsx_searcher_search_batch_mixed(gsx_searcher *s, const float *queries, int32_t nq, int32_t k,
@@ -177,8 +185,10 @@ typedef struct {
                                  check (staging applies to the integer kinds' rows of at most 128
                                  bytes and E5M2 rows of at most 256); bit 2: prefetch each
                                  neighbour's code row into L1 before its visited check (unstaged
-                                 rows); bit 1: load the predicted next adjacency row during the
-                                 merge; bit 0: also prefetch that row's code rows */
+                                 rows); bit 1: load the next adjacency row during the merge (the
+                                 merge settles the next pop before it moves pool entries); bit 0:
+                                 also prefetch that row's code rows; bit 5: also prefetch the
+                                 visited-table buckets of that row's neighbours */
     int32_t spill_bits;       /* log2 of the slots of each warp's global visited table (4 bytes a
                                  slot; 7..20, 0 = sized from the visit counts seen) */
 } gsx_tuning;
