@@ -74,54 +74,84 @@ int load_glass(const char *path, HostGraph &g) {
     return GSX_OK;
 }
 
-// NSG format (graph.hpp:354-379): K, ep, then per node (count, ids).
-int load_nsg(const char *path, HostGraph &g) {
-    std::ifstream f(path, std::ios::binary | std::ios::ate);
+// The whole file in memory (one read).  The row formats below (NSG, DiskANN) are parsed from it in
+// two passes: the first walks the (count, ids) records to count the rows and check every count, the
+// second copies each record into its -1-padded row.
+int read_all(const char *path, std::vector<char> &buf) {
+    FILE *f = std::fopen(path, "rb");
     if (!f) return fail(GSX_ERR_IO, "cannot open graph file '%s'", path);
-    const std::streamoff size = f.tellg();
-    f.seekg(0);
-    int32_t ep = 0;
-    if (!rd(f, &g.K) || !rd(f, &ep) || g.K <= 0) return fail(GSX_ERR_INVALID, "bad NSG header in '%s'", path);
-    if (g.K > kMaxDegree) return degree_unsupported(g.K);
-    g.eps.assign(1, ep);
-    std::vector<int32_t> buf;
-    std::vector<std::vector<int32_t>> rows;
-    while (f.tellg() < size) {
-        int32_t c = 0;
-        if (!rd(f, &c) || c < 0 || c > g.K) return fail(GSX_ERR_INVALID, "bad NSG row in '%s'", path);
-        buf.resize((size_t)c);
-        if (c && !rd(f, buf.data(), (size_t)c)) return fail(GSX_ERR_INVALID, "truncated NSG file '%s'", path);
-        rows.push_back(buf);
+    std::fseek(f, 0, SEEK_END);
+    const long size = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (size < 0) {
+        std::fclose(f);
+        return fail(GSX_ERR_IO, "cannot size graph file '%s'", path);
     }
-    g.N = (int32_t)rows.size();
-    g.adj.assign((size_t)g.N * g.K, -1);
-    for (int32_t i = 0; i < g.N; ++i) std::memcpy(&g.adj[(size_t)i * g.K], rows[i].data(), rows[i].size() * 4);
+    buf.resize((size_t)size);
+    const size_t got = size ? std::fread(buf.data(), 1, (size_t)size, f) : 0;
+    std::fclose(f);
+    if (got != (size_t)size) return fail(GSX_ERR_IO, "short read of graph file '%s'", path);
     return GSX_OK;
 }
 
-// DiskANN format (graph.hpp:289-316): u64 file size, K, ep, u64 frozen, then (count, ids) rows.
+// (count, ids) records starting before byte `end` of buf, from byte `at`, into g.adj (g.K set); as in
+// the reference's readers a record that starts before `end` is read whole.
+int parse_rows(const std::vector<char> &buf, size_t at, size_t end, HostGraph &g, const char *what, const char *path) {
+    if (end > buf.size()) end = buf.size();
+    const size_t total = buf.size();
+    size_t n = 0;
+    for (size_t p = at; p < end; ++n) {
+        int32_t c = 0;
+        if (total - p < 4) return fail(GSX_ERR_INVALID, "truncated %s file '%s'", what, path);
+        std::memcpy(&c, buf.data() + p, 4);
+        if (c < 0 || c > g.K) return fail(GSX_ERR_INVALID, "bad %s row %zu in '%s'", what, n, path);
+        if ((uint64_t)(total - p - 4) < (uint64_t)c * 4) return fail(GSX_ERR_INVALID, "truncated %s file '%s'", what, path);
+        p += 4 + (size_t)c * 4;
+    }
+    if (n == 0 || n > 0x7fffffffu) return fail(GSX_ERR_INVALID, "%s file '%s' holds %zu rows", what, path, n);
+    g.N = (int32_t)n;
+    g.adj.assign(n * (size_t)g.K, -1);
+    size_t p = at;
+    for (size_t i = 0; i < n; ++i) {
+        int32_t c = 0;
+        std::memcpy(&c, buf.data() + p, 4);
+        std::memcpy(&g.adj[i * (size_t)g.K], buf.data() + p + 4, (size_t)c * 4);
+        p += 4 + (size_t)c * 4;
+    }
+    return GSX_OK;
+}
+
+// NSG format (graph.hpp:354-379): K, ep, then per node (count, ids).
+int load_nsg(const char *path, HostGraph &g) {
+    std::vector<char> buf;
+    int rc = read_all(path, buf);
+    if (rc) return rc;
+    int32_t hdr[2] = {0, 0};
+    if (buf.size() < 8) return fail(GSX_ERR_INVALID, "bad NSG header in '%s'", path);
+    std::memcpy(hdr, buf.data(), 8);
+    g.K = hdr[0];
+    if (g.K <= 0) return fail(GSX_ERR_INVALID, "bad NSG header in '%s'", path);
+    if (g.K > kMaxDegree) return degree_unsupported(g.K);
+    g.eps.assign(1, hdr[1]);
+    return parse_rows(buf, 8, buf.size(), g, "NSG", path);
+}
+
+// DiskANN format (graph.hpp:289-316): u64 file size, K, ep, u64 frozen, then (count, ids) rows up to
+// the size the header states.
 int load_diskann(const char *path, HostGraph &g) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) return fail(GSX_ERR_IO, "cannot open graph file '%s'", path);
-    uint64_t size = 0, frozen = 0;
+    std::vector<char> buf;
+    int rc = read_all(path, buf);
+    if (rc) return rc;
+    if (buf.size() < 24) return fail(GSX_ERR_INVALID, "bad DiskANN header in '%s'", path);
+    uint64_t size = 0;
     int32_t ep = 0;
-    if (!rd(f, &size) || !rd(f, &g.K) || !rd(f, &ep) || !rd(f, &frozen) || g.K <= 0)
-        return fail(GSX_ERR_INVALID, "bad DiskANN header in '%s'", path);
+    std::memcpy(&size, buf.data(), 8);
+    std::memcpy(&g.K, buf.data() + 8, 4);
+    std::memcpy(&ep, buf.data() + 12, 4);
+    if (g.K <= 0) return fail(GSX_ERR_INVALID, "bad DiskANN header in '%s'", path);
     if (g.K > kMaxDegree) return degree_unsupported(g.K);
     g.eps.assign(1, ep);
-    std::vector<std::vector<int32_t>> rows;
-    std::vector<int32_t> buf;
-    while ((uint64_t)f.tellg() < size) {
-        int32_t c = 0;
-        if (!rd(f, &c) || c < 0 || c > g.K) return fail(GSX_ERR_INVALID, "bad DiskANN row in '%s'", path);
-        buf.resize((size_t)c);
-        if (c && !rd(f, buf.data(), (size_t)c)) return fail(GSX_ERR_INVALID, "truncated DiskANN file '%s'", path);
-        rows.push_back(buf);
-    }
-    g.N = (int32_t)rows.size();
-    g.adj.assign((size_t)g.N * g.K, -1);
-    for (int32_t i = 0; i < g.N; ++i) std::memcpy(&g.adj[(size_t)i * g.K], rows[i].data(), rows[i].size() * 4);
-    return GSX_OK;
+    return parse_rows(buf, 24, size < buf.size() ? (size_t)size : buf.size(), g, "DiskANN", path);
 }
 
 // hnswlib level-0 file (graph.hpp:318-352); multi-level files are refused as in the reference.
