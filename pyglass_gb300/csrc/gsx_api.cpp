@@ -846,7 +846,7 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
         if (t->table_bits != 0 && t->table_bits != kGlobalOnly && (t->table_bits < kMinTableBits || t->table_bits > 16))
             return fail(GSX_ERR_INVALID, "table_bits must be 0 (automatic), 1 (global table only) or in [%d, 16]",
                         kMinTableBits);
-        if (t->prefetch < 0 || t->prefetch > 31) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 31]");
+        if (t->prefetch < 0 || t->prefetch > 63) return fail(GSX_ERR_INVALID, "prefetch must be in [0, 63]");
         if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
             return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
         s->tuning = *t;
@@ -887,11 +887,23 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
         int auto_sb = 14;
         if (make_cfg(s, k, s->ef, nq, false, 0, &probe) == GSX_OK) auto_sb = spill_bits_for(s, probe);
         s->tuning.spill_bits = sb0;
+        // integer kinds whose code rows are staged in shared memory score them one lane per row
+        // whatever lanes_per_row says, so only one value is tried for them
+        LaunchCfg staged_probe;
+        if (make_cfg(s, k, s->ef, nq, false, 0, &staged_probe) == GSX_OK && staged_probe.L.stage_row > 0 &&
+            !is_float_kind(s->kind))
+            lprs = {1};
+        // row speculation (the merge settles the next pop and loads its row), with and without
+        // prefetching that row's code rows and visited-table buckets, against none
+        const int spec = kSpeculateRow;
+        const std::vector<int> pfs{0, kPrefetchNeighbours, spec, spec | kPrefetchCodes, spec | kPrefetchBuckets,
+                                   spec | kPrefetchCodes | kPrefetchBuckets};
         for (int wpb : {2, 4})
             for (int lpr : lprs)
                 for (int bits : bit_choices)
-                for (int pf : {0, 4})
-                for (int sb : {auto_sb, auto_sb + 1}) {
+                for (int pf : pfs)
+                for (int sb : {auto_sb - 1, auto_sb, auto_sb + 1}) {
+                    if (sb < kMinTableBits) continue;
                     gsx_tuning t{wpb, bits, lpr, pf, sb};
                     s->tuning = t;
                     float ms_min = 1e30f;

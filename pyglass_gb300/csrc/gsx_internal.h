@@ -43,6 +43,8 @@ constexpr int kNoStageCodes = 8;     // tuning.prefetch bit: do not stage neighb
                                      // most 128 bytes; E5M2 rows of at most 256)
 constexpr int kNoBatchOrder = 16;    // tuning.prefetch bit: run large batches in index order instead of
                                      // sorted by their principal-direction projection
+constexpr int kPrefetchBuckets = 32; // tuning.prefetch bit: once the next row has arrived, prefetch the
+                                     // visited-table buckets of its neighbours (global tables)
 constexpr int kOrderBins = 2048;     // bins of that sort
 
 // Device-resident index, as the kernels see it.
@@ -103,6 +105,7 @@ struct WarpLayout {
     int pool_key, pool_id, cand_id, cand_key, acc_ub, acc_key, acc_id, fq, qc, table;
     int stage;                // 32 code rows staged by cp.async (byte offset), when stage_row > 0
     int stage_row;            // bytes per staged row (the code size), 0 = no staging
+    int stage_stride;         // bytes between staged rows
     int total;                // bytes per warp (multiple of 16)
     int cap;                  // pool capacity available
     int fq_len;               // floats in the fp32 query buffer

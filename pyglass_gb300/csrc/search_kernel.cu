@@ -103,14 +103,19 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// First index in [lo, hi) whose entry is not yet expanded, or hi.
-__device__ __forceinline__ int first_unchecked(const int32_t *pid, int lo, int hi, int lane) {
+// First index in [lo, hi) whose entry is not yet expanded, or hi; `node` = its id (-1 when none).
+__device__ __forceinline__ int first_unchecked(const int32_t *pid, int lo, int hi, int lane, int32_t &node) {
     for (int base = lo; base < hi; base += 32) {
-        int i = base + lane;
-        bool un = i < hi && pid[i] >= 0;
-        unsigned b = __ballot_sync(kFull, un);
-        if (b) return base + __ffs(b) - 1;
+        const int i = base + lane;
+        const int32_t v = i < hi ? pid[i] : -1;  // bit 31 set: expanded (or past the range)
+        const unsigned b = __ballot_sync(kFull, v >= 0);
+        if (b) {
+            const int src = __ffs(b) - 1;
+            node = __shfl_sync(kFull, v, src);
+            return base + src;
+        }
     }
+    node = -1;
     return hi;
 }
 
@@ -216,22 +221,54 @@ __device__ __forceinline__ void migrate_visited(WarpState &w, int lane, bool &ba
     __syncwarp();
 }
 
-// merge() for at most 32 surviving candidates (cand_{key,id}[0..ns), arrival order) and a pool of
-// at most 32*GS entries (GS = 4 or 8), in registers.  Candidate j (lane j): rank_j among the
-// candidates, ub_j = pool entries with key <= key_j, found from the last keys of the pool's
-// GS-entry groups (one ballot per candidate) and one read of its group; slot_j = ub_j + rank_j.
-// Pool entry p moves to p + #{candidates c: ub_c <= p} (the candidates with smaller keys).  The
-// entries from the first candidate's slot up move in blocks of 128 from the top down: a block is
-// read whole, then written, and its entries only move up into blocks already read; whatever lands
-// at cap or beyond is dropped.
+// The pop of the next expansion, settled by the merge before it moves any pool entry: its pool index
+// (exact: the first unexpanded entry of the merged pool) and its node, whose adjacency row is
+// loaded right away when speculation is on, so that it arrives while the merge runs.
+struct NextPop {
+    int f = -1;                // pool index of the next pop; -1 = not known (the loop top looks it up)
+    int32_t node = -1;         // its node (valid when f is below the expansion limit)
+    int u = -1;                // its node when its row was loaded (-1: nothing loaded)
+    int32_t r0 = -1, r1 = -1;  // that row: entries lane and 32 + lane
+};
+
+// f0 = first unexpanded index of the pool before the merge (lim if none below min(S, lim)) and node0
+// its node, lo = the slot of the best candidate that enters (INT_MAX when none does).  The merged
+// pool's first unexpanded entry is the candidate when lo <= f0 (it lands at or before f0's entry),
+// else f0's entry, which no candidate passes.  `cand` is the candidate's node (used when lo <= f0).
+__device__ __forceinline__ void settle_next(const IndexView &ix, NextPop &np, bool speculate, int f0, int32_t node0,
+                                            int lo, int lim, int32_t cand, int lane) {
+    const int f = lo <= f0 ? lo : f0;
+    const int32_t u = lo <= f0 ? cand : node0;
+    np.f = f;
+    np.node = u;
+    np.u = -1;
+    if (!speculate || f >= lim || u < 0) return;
+    const int32_t *row = ix.adj + (size_t)u * (size_t)ix.K;
+    np.u = u;
+    np.r0 = lane < ix.K ? __ldg(row + lane) : -1;
+    np.r1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
+}
+
+// merge() for at most 32 surviving candidates (cand_{key,id}[0..ns), arrival order) and a pool of at
+// most 32*GS entries (GS = 4 or 8).  Candidate j (lane j): rank_j among the candidates by (key,
+// arrival), and ub_j = pool entries with key <= key_j, found from the last keys of the pool's
+// GS-entry groups (one ballot per candidate) and one read of its group; its slot is ub_j + rank_j,
+// taken when below cap (slots rise with rank, so the taken candidates are ranks 0..n-1).  The pool
+// from the first slot up is then rebuilt in one parallel pass: the taken slots are gathered into
+// 32-position bit words (redux.or), so for every position q the number c of taken slots below q is
+// a prefix popcount; q holds the candidate of rank c when it is a taken slot, else the old entry
+// q - c.  Every position reads before any writes, and whatever lands at cap or beyond is dropped.
 template <int GS>
-__device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &lb, int m, int ns, int lane) {
+__device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &lb, int m, int ns, int lane,
+                                            const IndexView &ix, NextPop *np, bool speculate, int f0, int32_t node0,
+                                            int lim) {
     const bool has = lane < ns;
     const uint32_t kj = has ? w.cand_key[lane] : 0xffffffffu;
     const int32_t ij = has ? w.cand_id[lane] : 0;
     const bool full = GS * lane + GS - 1 < S;
     const uint32_t piv = full ? w.pkey[GS * lane + GS - 1] : 0u;
     int rank = 0, grp = 0;
+#pragma unroll 4
     for (int i = 0; i < ns; ++i) {
         const uint32_t ki = __shfl_sync(kFull, kj, i);
         const unsigned b = __ballot_sync(kFull, full && piv <= ki);
@@ -257,44 +294,61 @@ __device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &
     // the rank-0 candidate always fits (its key is below the last entry of a full pool)
     const int lo = (int)__reduce_min_sync(kFull, acc ? (unsigned)slot : 0x7fffffffu);
     const int sl = __popc(__ballot_sync(kFull, has && ub <= lb));
-    // pool entries in [lo, S), 128 at a time from the top (four per lane) and how far each moves
-    for (int blk = S > lo ? (S - 1 - lo) >> 7 : -1; blk >= 0; --blk) {
-        uint32_t pk[4];
-        int32_t pi[4];
-        int pp[4], sh[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            pp[t] = lo + 128 * blk + lane + 32 * t;
-            sh[t] = 0;
-            const bool in = pp[t] < S;
-            pk[t] = in ? w.pkey[pp[t]] : 0u;
-            pi[t] = in ? w.pid[pp[t]] : 0;
-        }
-        for (int i = 0; i < ns; ++i) {
-            const int ui = __shfl_sync(kFull, ub, i);
-#pragma unroll
-            for (int t = 0; t < 4; ++t) sh[t] += ui <= pp[t];
-        }
-        __syncwarp();
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const int q = pp[t] + sh[t];
-            if (pp[t] < S && sh[t] > 0 && q < cap) {
-                w.pkey[q] = pk[t];
-                w.pid[q] = pi[t];
-            }
-        }
-        __syncwarp();
+    if (np) {
+        // the rank-0 candidate holds slot lo; its node is the next pop when lo <= f0
+        const unsigned r0 = __ballot_sync(kFull, acc && slot == lo);
+        const int32_t cand = __shfl_sync(kFull, ij, r0 ? __ffs(r0) - 1 : 0);
+        settle_next(ix, *np, speculate, f0, node0, lo, lim, cand, lane);
     }
     if (acc) {
-        w.pkey[slot] = kj;
-        w.pid[slot] = ij;
+        w.acc_key[rank] = kj;
+        w.acc_id[rank] = ij;
+    }
+    const int newS = (S + m) < cap ? (S + m) : cap;
+    // positions below 32 * (GS + 1) hold every slot: S <= 32 * GS and at most 32 candidates
+    constexpr int NW = GS + 1;
+    uint32_t word[NW];
+#pragma unroll
+    for (int t = 0; t < NW; ++t)
+        word[t] = __reduce_or_sync(kFull, (acc && (slot >> 5) == t) ? 1u << (slot & 31) : 0u);
+    __syncwarp();
+    const unsigned ltm = lanemask_lt();
+    uint32_t nk[NW];
+    int32_t ni[NW];
+    int before = 0;
+#pragma unroll
+    for (int t = 0; t < NW; ++t) {
+        const int q = 32 * t + lane;
+        nk[t] = 0u;
+        ni[t] = 0;
+        if (32 * t + 31 >= lo && 32 * t < newS) {
+            const int c = before + __popc(word[t] & ltm);
+            if (q >= lo && q < newS) {
+                if ((word[t] >> lane) & 1u) {
+                    nk[t] = w.acc_key[c];
+                    ni[t] = w.acc_id[c];
+                } else {
+                    nk[t] = w.pkey[q - c];
+                    ni[t] = w.pid[q - c];
+                }
+            }
+        }
+        before += __popc(word[t]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < NW; ++t) {
+        const int q = 32 * t + lane;
+        if (32 * t + 31 >= lo && 32 * t < newS && q >= lo && q < newS) {
+            w.pkey[q] = nk[t];
+            w.pid[q] = ni[t];
+        }
     }
     // new lower bound of the first unexpanded entry: the first candidate, or where the old bound
     // moved to
     const int nl = lb + sl;
     lb = lo < nl ? lo : nl;
-    S = (S + m) < cap ? (S + m) : cap;
+    S = newS;
     __syncwarp();
 }
 
@@ -310,7 +364,12 @@ __device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &
 // redux.or of the candidates' slot bits in the chunk says which slots take a candidate, and every
 // other slot p takes the pool entry p - (candidates placed below p).  A chunk only reads entries
 // at or below its own slots, so no entry is overwritten before it is read.
-__device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, int m, int lane) {
+//
+// With np given, f0 is the first unexpanded index before the merge (lim if none below min(S, lim)),
+// node0 its node, and the next expansion's pop is settled (settle_next) before any entry moves.
+__device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, int m, int lane,
+                                      const IndexView &ix, NextPop *np = nullptr, bool speculate = false, int f0 = 0,
+                                      int32_t node0 = -1, int lim = 0) {
     // survivors: with a full pool a candidate whose key is not below the last entry can never
     // enter, and its larger key does not change the rank of one that does
     const unsigned ltm = (1u << lane) - 1u;
@@ -323,6 +382,7 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     const int ns = __popc(b0) + __popc(b1);
     if (ns == 0) {
         S = (S + m) < cap ? (S + m) : cap;
+        if (np) settle_next(ix, *np, speculate, f0, node0, 0x7fffffff, lim, -1, lane);
         return;
     }
     // compact the survivors in arrival order
@@ -339,11 +399,11 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     }
     __syncwarp();
     if (ns <= 32 && S <= 128) {
-        merge_small<4>(w, S, cap, lb, m, ns, lane);
+        merge_small<4>(w, S, cap, lb, m, ns, lane, ix, np, speculate, f0, node0, lim);
         return;
     }
     if (ns <= 32 && S <= 256) {
-        merge_small<8>(w, S, cap, lb, m, ns, lane);
+        merge_small<8>(w, S, cap, lb, m, ns, lane, ix, np, speculate, f0, node0, lim);
         return;
     }
     int nacc = 0;
@@ -370,7 +430,10 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
         if (ns <= 32) break;
     }
     __syncwarp();
-    if (nacc == 0) return;
+    if (nacc == 0) {  // cannot happen: the rank-0 survivor always fits
+        if (np) settle_next(ix, *np, speculate, f0, node0, 0x7fffffff, lim, -1, lane);
+        return;
+    }
     // slots of the accepted candidates, rank r held by lane r (and r+32)
     constexpr int kNone = 0x7fffffff;
     const int ub0 = lane < nacc ? w.acc_ub[lane] : kNone;
@@ -378,6 +441,7 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     const int p0 = ub0 == kNone ? kNone : ub0 + lane;
     const int p1 = ub1 == kNone ? kNone : ub1 + lane + 32;
     const int lo = __shfl_sync(kFull, p0, 0);  // slot of the rank-0 candidate = acc_ub[0]
+    if (np) settle_next(ix, *np, speculate, f0, node0, lo, lim, w.acc_id[0], lane);
     const int newS = (S + m) < cap ? (S + m) : cap;
     const int nchunks = (newS - lo + 31) >> 5;
     for (int c = nchunks - 1; c >= 0; --c) {
@@ -455,37 +519,6 @@ __device__ __forceinline__ void refine_dists(const IndexView &ix, const int32_t 
         if (act && sub == 0) out[j] = dv;
     }
     __syncwarp();
-}
-
-// The node the next expansion will pop, known before the merge: the first unexpanded pool entry,
-// unless the best candidate that can enter has a strictly smaller key (equal keys go after the
-// pool entry).  Used only to start loading that node's adjacency row early; the pop checks it.
-__device__ __forceinline__ int predict_next(const WarpState &w, int S, int cap, int lb, int lim, int m, int lane) {
-    const int hi = S < lim ? S : lim;
-    const int f0 = first_unchecked(w.pid, lb, hi, lane);
-    const bool has_pool = f0 < hi;
-    const uint32_t kf = has_pool ? w.pkey[f0] : 0xffffffffu;
-    const uint32_t last = S == cap ? w.pkey[S - 1] : 0xffffffffu;
-    uint32_t bk = 0xffffffffu;
-    int bj = kMaxDegree;
-    for (int j = lane; j < m; j += 32) {
-        const uint32_t k = w.cand_key[j];
-        if ((S < cap || k < last) && (k < bk || (k == bk && j < bj))) {
-            bk = k;
-            bj = j;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const uint32_t ok = __shfl_xor_sync(kFull, bk, o);
-        const int oj = __shfl_xor_sync(kFull, bj, o);
-        if (ok < bk || (ok == bk && oj < bj)) {
-            bk = ok;
-            bj = oj;
-        }
-    }
-    if (bj < kMaxDegree && (!has_pool || bk < kf)) return w.cand_id[bj];
-    return has_pool ? (w.pid[f0] & kIdMask) : -1;
 }
 
 // Encodes the query held in w.fq into w.qc (SQ kinds); returns the sum of squared codes.
@@ -637,7 +670,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             w.cand_key[0] = cur;
         }
         __syncwarp();
-        merge(w, S, cap, lb, 1, lane);
+        merge(w, S, cap, lb, 1, lane, ix);
         bool bad = false;
         visit_all(w, lane == 0, u, bad);
         nvis += 1;
@@ -650,7 +683,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             __syncwarp();
             compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
             cmps += m;
-            merge(w, S, cap, lb, m, lane);
+            merge(w, S, cap, lb, m, lane, ix);
             bool bad = false;
             for (int j0 = 0; j0 < m; j0 += 32) {
                 const int j = j0 + lane;
@@ -665,10 +698,11 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
 
     // ---- SearchImpl2 (graph_searcher.hpp:196-224) ----
     const int lim = ef_expand < cap ? ef_expand : cap;
-    int pred_u = -1;             // node whose row was loaded speculatively during the last merge
-    int32_t pv0 = -1, pv1 = -1;  // that row: entries lane and 32 + lane
+    const bool speculate = (L.prefetch & kSpeculateRow) != 0;
+    NextPop np;  // the pop the last merge settled, with its row when it was loaded
     while (!overflow) {
-        const int f = first_unchecked(w.pid, lb, S < lim ? S : lim, lane);
+        int32_t u = np.node;
+        const int f = np.f >= 0 ? np.f : first_unchecked(w.pid, lb, S < lim ? S : lim, lane, u);
         if (f >= S || f >= lim) break;
         if (nvis + ix.K > tlimit) {
             if (w.spill && w.epoch == 0) {
@@ -679,19 +713,19 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             }
             if (nvis + ix.K > tlimit) { overflow = true; break; }
         }
-        const int32_t raw = w.pid[f];
-        __syncwarp();
-        if (lane == 0) w.pid[f] = raw | kChecked;
-        const int u = raw & kIdMask;
+        // the pop (neighbor.hpp:398-405): the entry is unexpanded, so its stored id is u itself
+        if (lane == 0) w.pid[f] = u | kChecked;
         lb = f + 1;
         ++nexp;
         // adjacency row, stop at the first -1; skip repeats within the row and visited ids
-        int32_t r0 = pv0, r1 = pv1;
-        if (u != pred_u) {
+        int32_t r0 = np.r0, r1 = np.r1;
+        if (u != np.u) {
             const int32_t *row = ix.adj + (size_t)u * (size_t)ix.K;
             r0 = lane < ix.K ? __ldg(row + lane) : -1;
             r1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
         }
+        np.f = -1;
+        np.u = -1;
         int m = 0;
         const bool staged = L.stage_row > 0;
         for (int c0 = 0; c0 < ix.K; c0 += 32) {
@@ -705,7 +739,7 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             uint8_t *srow = nullptr;
             if (staged) {
                 // copy the code row into shared memory now, so that it arrives during the visited check
-                srow = w.stage + lane * L.stage_row;
+                srow = w.stage + lane * L.stage_stride;
                 if (first) {
                     const uint8_t *c = ix.codes + (size_t)v * (size_t)ix.csize;
                     for (int o = 0; o < L.stage_row; o += 16) cp_async16(srow + o, c + o);
@@ -743,33 +777,31 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
         }
         __syncwarp();
         nvis += m;
-        if (m == 0) {
-            pred_u = -1;
-            continue;
-        }
+        if (m == 0) continue;
         if (!staged) compute_dists<KIND, METRIC, LPR>(ix, w, m, qsq, lane);
         cmps += m;
-        // start the next row's load now, so that it arrives while the merge runs
-        pred_u = (L.prefetch & kSpeculateRow) ? predict_next(w, S, cap, lb, lim, m, lane) : -1;
-        if (pred_u >= 0) {
-            const int32_t *row = ix.adj + (size_t)pred_u * (size_t)ix.K;
-            pv0 = lane < ix.K ? __ldg(row + lane) : -1;
-            pv1 = lane + 32 < ix.K ? __ldg(row + 32 + lane) : -1;
-        }
-        merge(w, S, cap, lb, m, lane);
-        if ((L.prefetch & kPrefetchCodes) && pred_u >= 0) {
-            // the predicted row has arrived during the merge: pull its neighbours' code rows
-            // towards L1 for the next expansion (a wrong prediction only wastes the prefetch;
-            // cf. the reference's computer.prefetch, graph_searcher.hpp:212-218)
+        // the merge settles the next pop (and, speculating, starts loading its row) before it moves
+        // pool entries
+        int32_t node0;
+        const int f0 = first_unchecked(w.pid, lb, S < lim ? S : lim, lane, node0);
+        merge(w, S, cap, lb, m, lane, ix, &np, speculate, f0, node0, lim);
+        if ((L.prefetch & kPrefetchCodes) && np.u >= 0) {
+            // the next row has arrived during the merge: pull its neighbours' code rows towards L1
+            // for the next expansion (cf. the reference's computer.prefetch, graph_searcher.hpp:212-218)
             const int lines = ix.csize > 128 ? 2 : 1;
-            if (pv0 >= 0) {
-                const uint8_t *c = ix.codes + (size_t)pv0 * (size_t)ix.csize;
+            if (np.r0 >= 0) {
+                const uint8_t *c = ix.codes + (size_t)np.r0 * (size_t)ix.csize;
                 for (int l = 0; l < lines; ++l) asm volatile("prefetch.global.L1 [%0];" ::"l"(c + 128 * l));
             }
-            if (pv1 >= 0) {
-                const uint8_t *c = ix.codes + (size_t)pv1 * (size_t)ix.csize;
+            if (np.r1 >= 0) {
+                const uint8_t *c = ix.codes + (size_t)np.r1 * (size_t)ix.csize;
                 for (int l = 0; l < lines; ++l) asm volatile("prefetch.global.L1 [%0];" ::"l"(c + 128 * l));
             }
+        }
+        if ((L.prefetch & kPrefetchBuckets) && np.u >= 0 && w.epoch) {
+            // the first buckets the next expansion's visited check reads, towards L1 (the warp's own table)
+            if (np.r0 >= 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.spill + 8 * slot_of(np.r0, w.sbits - 3)));
+            if (np.r1 >= 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.spill + 8 * slot_of(np.r1, w.sbits - 3)));
         }
     }
 
@@ -1063,10 +1095,15 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
     const bool int_kind = ix.kind == K_SQ4U || ix.kind == K_SQ8U || ix.kind == K_SQ2U || ix.kind == K_SQ4UA ||
                           ix.kind == K_SQ1;
     const bool small_float = ix.kind == K_E5M2;
+    L->stage_stride = 0;
     if ((int_kind || small_float) && !(prefetch & kNoStageCodes) && ix.csize <= (int_kind ? 128 : 256) &&
         ix.csize % 16 == 0) {
+        // rows 16 bytes apart beyond their size: a lane's 16-byte reads of its own row then fall on
+        // other banks than its neighbours' (a stride that is a multiple of 64 bytes puts four lanes of
+        // every quarter warp on the same banks)
         L->stage_row = ix.csize;
-        off += 32 * ix.csize;
+        L->stage_stride = ix.csize + 16;
+        off += 32 * L->stage_stride;
     }
     L->total = up(off, 16);
     L->cap = capa - 1;

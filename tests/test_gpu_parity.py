@@ -146,7 +146,7 @@ def test_tuning_variants_agree(gpu, golden):
     try:
         for wpb in (1, 2, 8):
             for lpr in (1, 2, 4):
-                for prefetch in (0, 1, 2, 3, 4, 7, 8, 12):  # 8: code rows not staged
+                for prefetch in (0, 1, 2, 3, 4, 7, 8, 12, 34, 35):  # 8: code rows not staged; 32: buckets
                     for bits in (0, 1, 9):  # automatic, global table only, 512 shared slots
                         s.set_tuning(warps_per_block=wpb, table_bits=bits, lanes_per_row=lpr, prefetch=prefetch,
                                      spill_bits=0)
