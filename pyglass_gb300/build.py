@@ -25,10 +25,10 @@ EXT = os.path.join(PKG, "_glass" + (sysconfig.get_config_var("EXT_SUFFIX") or ".
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["search_kernel.cu", "encode_kernel.cu", "order_kernel.cu", "calib_kernel.cu", "noalloc.cu", "knn_kernel.cu",
+CUDA_SOURCES = ["search_kernel.cu", "search_fast.cu", "encode_kernel.cu", "order_kernel.cu", "calib_kernel.cu", "noalloc.cu", "knn_kernel.cu",
                 "build_kernel.cu"]
 HOST_SOURCES = ["gsx_api.cpp", "gsx_graph.cpp", "gsx_server.cpp", "gsx_capture.cpp"]
-HEADERS = ["gsx_internal.h", "gsx_device.cuh", "gsx_host.h", "gsx_ranges.h"]
+HEADERS = ["gsx_internal.h", "gsx_device.cuh", "gsx_host.h", "gsx_ranges.h", "search_core.cuh"]
 
 
 def _newer(out: str, deps: list[str]) -> bool:

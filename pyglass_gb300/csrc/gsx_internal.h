@@ -108,6 +108,7 @@ struct WarpLayout {
     int stage_stride;         // bytes between staged rows
     int total;                // bytes per warp (multiple of 16)
     int cap;                  // pool capacity available
+    int pool_cap;             // largest pool capacity max(k * factor, ef) the launch's queries use
     int fq_len;               // floats in the fp32 query buffer
     int table_bits;           // 0 => visited table in global memory (BatchView::gtab)
     int prefetch;
@@ -127,6 +128,11 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
 // Kernel launchers (search_kernel.cu).  Return cudaGetLastError() of the launch.
 cudaError_t launch_search(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st);
 int search_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg);
+// The fast form (search_fast.cu) for integer codes staged as 64- or 128-byte rows, degree <= 32,
+// visited sets in global tables only and pools of at most 128 entries; same results.
+bool search_fast_fits(const IndexView &ix, const LaunchCfg &cfg);
+cudaError_t launch_search_fast(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st);
+int search_fast_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg);
 
 // Encoding and distance kernels (encode_kernel.cu).
 cudaError_t launch_encode(int kind, int metric, const float *data, int64_t n, int d, int dalign, int csize, float p0,
