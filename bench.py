@@ -50,6 +50,9 @@ def args_():
                    help="only the GPU NSG build of the first ROWS base rows (for ncu launch lists)")
     p.add_argument("--profile", action="store_true",
                    help="only the warm-up and timed device launches (default tuning), for ncu captures")
+    p.add_argument("--case", default=None, choices=sorted(CASES),
+                   help="one small case of other kernels (for ncu captures): " + "; ".join(
+                       f"{k}: {v[0]}" for k, v in sorted(CASES.items())))
     return p.parse_args()
 
 
@@ -523,6 +526,40 @@ def run_gpu(a):
                       "avg_dist_cmps": float(cmps.float().mean().item())})
     s.set_ef(a.ef)
 
+    # the same search over 100,000 queries (the 10,000 repeated ten times) in one launch: about twenty
+    # queries per resident warp, so the steady state shows apart from the 10,000-query batch's tail
+    rep = 10
+    dq_w = dq.repeat(rep, 1)
+    nw = dq_w.shape[0]
+    ids_w = torch.empty((nw, K), dtype=torch.int32, device="cuda")
+    dis_w = torch.empty((nw, K), dtype=torch.float32, device="cuda")
+    cm_w = torch.empty(nw, dtype=torch.int32, device="cuda")
+    ex_w = torch.empty(nw, dtype=torch.int32, device="cuda")
+
+    def launch_w():
+        s.batch_search_device(dq_w.data_ptr(), nw, K, ids_w.data_ptr(), dis_w.data_ptr(), cmps=cm_w.data_ptr(),
+                              expansions=ex_w.data_ptr(), kmax=K, stream=stream.cuda_stream)
+
+    launch_w()
+    w_ms = []
+    for _ in range(3):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch_w()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        w_ms.append(e0.elapsed_time(e1))
+    cw = cm_w.cpu().numpy().astype(np.int64)
+    xw = ex_w.cpu().numpy().astype(np.int64)
+    bytes_w = int((cw * csize).sum() + (xw * 4 * Kdeg).sum() + nw * (reorder * 4 * 128 + 4 * d + 8 * K))
+    ach_w = bytes_w / (statistics.mean(w_ms) / 1000.0) / 1e9
+    multiwave = {"nq": nw, "ms": statistics.mean(w_ms), "qps": nw / (statistics.mean(w_ms) / 1000.0),
+                 "roofline_frac": ach_w / peak, "achieved_gbs": ach_w,
+                 "same_ids_as_headline": bool(np.array_equal(ids_w.cpu().numpy()[:nq], out_ids)),
+                 "overflowed_queries": s.overflow_count()}
+    del dq_w, ids_w, dis_w, cm_w, ex_w
+
     # e2e: the public API with host buffers (copies in the timed region)
     for _ in range(2):
         s.batch_search(queries, K)
@@ -593,6 +630,7 @@ def run_gpu(a):
                          "avg_expansions": float(x.mean())},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": a.steps * launches_per_step, "clocks": clk.summary(),
             "plain_per_query": plain, "batched_over_plain": value / world / plain["qps"], "sweep": sweep,
+            "multiwave_100k": multiwave,
             "ground_truth": gt_info, "serving": serving, "graph_build": build, "cuda_graph_replay": replay,
         }
         print(json.dumps(line))
@@ -600,8 +638,85 @@ def run_gpu(a):
         dist.destroy_process_group()
 
 
+def _case_search(workload, metric, quant, refine, ef, k, nq, launches):
+    """Loads a workload's graph and rows, runs `launches` timed device batches of nq queries and
+    returns the mean ms per launch (CUDA events on the launching stream)."""
+    import torch
+
+    from pyglass_gb300 import datasets, glass
+
+    found = datasets.graph_file(workload, ROOT)
+    if found is None:
+        raise SystemExit(json.dumps({"error": f"data/{workload} graph absent (oracle/build_graphs.py {workload})"}))
+    w = datasets.WORKLOADS[workload]
+    base, queries = w["base"](), w["queries"]()[:nq]
+    s = glass.Searcher(glass.Graph(*found), base, metric, quant, refine)
+    s.set_ef(ef)
+    s.batch_search(queries, k)
+    stream = torch.cuda.Stream()
+    dq = torch.from_numpy(queries).cuda()
+    ids = torch.empty((nq, k), dtype=torch.int32, device="cuda")
+    dis = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+    ms = []
+    for _ in range(launches):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.batch_search_device(dq.data_ptr(), nq, k, ids.data_ptr(), dis.data_ptr(), kmax=k, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return {"workload": workload, "quantizer": quant, "refine": refine, "metric": metric, "ef": ef, "k": k, "nq": nq,
+            "ms_per_launch": ms, "tuning": s.get_tuning()}
+
+
+def _case_setdata():
+    """SetData of the 1M x 128 rows for every encoder family (calibration, encoding, padding), then
+    one 10,000-query batch (batch-order kernels and the search)."""
+    import torch
+
+    from pyglass_gb300 import datasets, glass
+
+    w = datasets.WORKLOADS[WORKLOAD]
+    base, queries = w["base"](), w["queries"]()
+    g = glass.Graph(*graph_file())
+    out = {}
+    for quant, refine in (("SQ4U", "FP32"), ("SQ8U", ""), ("SQ8", ""), ("FP16", ""), ("E5M2", "")):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s = glass.Searcher(g, base, "L2", quant, refine)
+        torch.cuda.synchronize()
+        out[f"{quant}{'+' + refine if refine else ''}_setdata_s"] = time.perf_counter() - t
+        if quant == "SQ4U":
+            s.set_ef(128)
+            s.batch_search(queries, K)
+        del s
+    return out
+
+
+CASES = {
+    "setdata": ("SetData of 1M x 128 rows for SQ4U+FP32, SQ8U, SQ8, FP16, E5M2 and one 10,000-query SQ4U batch",
+                _case_setdata),
+    "lowrank-e5m2": ("100,000 x 960 low-rank rows, HNSW R=32 L=200, E5M2, ef 128, 1,000 queries",
+                     lambda: _case_search("lowrank100k", "L2", "E5M2", "", 128, 10, 1000, 5)),
+    "lowrank-sq8u": ("100,000 x 960 low-rank rows, HNSW R=32 L=200, SQ8U, ef 128, 1,000 queries",
+                     lambda: _case_search("lowrank100k", "L2", "SQ8U", "", 128, 10, 1000, 5)),
+    "sphere-sq4u-ip": ("200,000 x 768 unit rows, NSG R=48 L=100, inner product, SQ4U + FP32 refine, ef 128, "
+                       "2,000 queries", lambda: _case_search("sphere200k", "IP", "SQ4U", "FP32", 128, 10, 2000, 5)),
+}
+
+
+def run_case(a):
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps({"case": a.case, "what": CASES[a.case][0], **CASES[a.case][1]()}))
+
+
 def main():
     a = args_()
+    if a.case:
+        run_case(a)
+        return
     if a.impl == "reference":
         run_reference(a)
     else:
