@@ -62,17 +62,25 @@ def normalized_mixture(n: int, d: int = 768, n_clusters: int = 4096, sigma: floa
                        stream: int = 0) -> np.ndarray:
     """Unit-length rows of a Gaussian mixture (centers ~ N(0, I), within-cluster sigma).
 
-    The row norms are sums of float64 squares taken column by column in a fixed order, and every
-    other step is one correctly rounded elementwise operation, so x86 and aarch64 hosts produce the
-    same bytes (a float32 ``np.linalg.norm`` reduces in SIMD-width-dependent order and does not)."""
-    centers = np.random.default_rng([seed, 999]).standard_normal((n_clusters, d), dtype=np.float32)
+    Every random value is built from integer-derived uniforms by correctly rounded arithmetic alone,
+    so x86 and aarch64 hosts produce the same bytes: a normal deviate is a centred, scaled sum of four
+    uniforms (numpy's ziggurat samplers call libm's exp and log, whose last bits differ between hosts,
+    and a flipped accept/reject decision desynchronises the stream), and the row norms are sums of
+    float64 squares taken column by column in a fixed order (a float32 ``np.linalg.norm`` reduces in
+    SIMD-width-dependent order)."""
+
+    def normals(rng, shape):
+        u = rng.random((4,) + shape)
+        return (u[0] + u[1] + u[2] + u[3] - 2.0) * np.sqrt(3.0)
+
+    centers = normals(np.random.default_rng([seed, 999]), (n_clusters, d))
     rng = np.random.default_rng([seed, stream])
     out = np.empty((n, d), np.float32)
-    for s in range(0, n, _CHUNK):
-        m = min(_CHUNK, n - s)
+    step = 20_000
+    for s in range(0, n, step):
+        m = min(step, n - s)
         lab = rng.integers(0, n_clusters, size=m)
-        x = centers[lab] + rng.standard_normal((m, d), dtype=np.float32) * np.float32(sigma)
-        xt = np.ascontiguousarray(x.T).astype(np.float64)
+        xt = np.ascontiguousarray((centers[lab] + normals(rng, (m, d)) * sigma).T)
         ss = np.zeros(m)
         for j in range(d):
             ss += xt[j] * xt[j]
