@@ -129,7 +129,7 @@ bool make_layout(const IndexView &ix, int cap, int table_bits, int prefetch, War
 cudaError_t launch_search(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st);
 int search_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg);
 // The fast form (search_fast.cu) for integer codes staged as 64- or 128-byte rows, degree <= 32,
-// visited sets in global tables only and pools of at most 128 entries; same results.
+// visited sets in global tables only and pools of at most 256 entries; same results.
 bool search_fast_fits(const IndexView &ix, const LaunchCfg &cfg);
 cudaError_t launch_search_fast(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st);
 int search_fast_max_blocks_per_sm(const IndexView &ix, const LaunchCfg &cfg);

@@ -87,17 +87,21 @@ __device__ __forceinline__ void store_slot(uint32_t *p, uint32_t v) {
 
 constexpr int kBucketFull = 16;
 
-// Slot of the first match or free slot in a bucket: 0..7 = a free slot, 8..15 = v found (8 +
-// slot), kBucketFull = the bucket holds eight other ids.  Inserts take the first free slot along
-// the probe sequence and slots are never freed under one tag, so a free slot before v means v
-// is absent.
+// What one bucket says about `mine` (= tag << shift | id): 0..7 = not there, and its first free slot;
+// 8 = already there; kBucketFull = the bucket holds eight other ids.  Tags only grow between two
+// clears of the table, so a slot is the current query's exactly when it is >= tag << shift; and
+// inserts take the first free slot along the probe sequence and never free one under a tag, so the
+// current query's slots are a prefix of the bucket and their count is the first free slot.
 __device__ __forceinline__ int scan_bucket(const Bucket &b, uint32_t mine, int shift, uint32_t tag) {
+    const uint32_t base = tag << shift;
+    bool found = false;
+    int n = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-        if (b.e[j] == mine) return 8 + j;
-        if ((b.e[j] >> shift) != tag) return j;
+        found |= b.e[j] == mine;
+        n += b.e[j] >= base;
     }
-    return kBucketFull;
+    return found ? 8 : (n < 8 ? n : kBucketFull);
 }
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
@@ -371,7 +375,7 @@ __device__ __forceinline__ void merge_small(WarpState &w, int &S, int cap, int &
 //
 // With np given, f0 is the first unexpanded index before the merge (lim if none below min(S, lim)),
 // node0 its node, and the next expansion's pop is settled (settle_next) before any entry moves.
-template <bool SMALL = false>  // SMALL: at most 32 candidates and a pool of at most 128 entries
+template <bool SMALL = false>  // SMALL: at most 32 candidates and a pool of at most 256 entries
 __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, int m, int lane,
                                       const IndexView &ix, NextPop *np = nullptr, bool speculate = false, int f0 = 0,
                                       int32_t node0 = -1, int lim = 0) {
@@ -403,15 +407,15 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
         w.cand_id[t] = i1;
     }
     __syncwarp();
-    if (SMALL || (ns <= 32 && S <= 128)) {
+    if (ns <= 32 && S <= 128) {
         merge_small<4>(w, S, cap, lb, m, ns, lane, ix, np, speculate, f0, node0, lim);
         return;
     }
-    if constexpr (SMALL) return;
-    if (ns <= 32 && S <= 256) {
+    if (SMALL || (ns <= 32 && S <= 256)) {
         merge_small<8>(w, S, cap, lb, m, ns, lane, ix, np, speculate, f0, node0, lim);
         return;
     }
+    if constexpr (SMALL) return;
     int nacc = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -581,7 +585,7 @@ __device__ __forceinline__ int32_t prepare_query(const IndexView &ix, WarpState 
 
 // NCH > 0 compiles the fast form of the expansion loop for the common shapes: integer codes staged in
 // shared memory as NCH 16-byte chunks, degree <= 32, visited sets in the warps' global tables and pools
-// of at most 128 entries (the host launches it only then).  The search is the same; only the runtime
+// of at most 256 entries (the host launches it only then).  The search is the same; only the runtime
 // tests of the general form become compile-time facts.
 template <int KIND, int METRIC, int LPR, int NCH>
 __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpLayout &L, WarpState &w, int qi,
@@ -745,9 +749,15 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             const unsigned endm = __ballot_sync(kFull, v == -1);
             const int nvalid = endm ? __ffs(endm) - 1 : 32;
             const bool valid = lane < nvalid;
-            const unsigned same = __match_any_sync(kFull, v);
-            const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
-            const bool first = valid && ((same & vmask & lanemask_lt()) == 0);
+            // repeats inside the row: the first occurrence is the one visited (the reference checks
+            // and sets the bitset neighbour by neighbour).  The fast form leaves this to the global
+            // table, whose inserts already go to the lowest of the lanes holding one id.
+            bool first = valid;
+            if constexpr (NCH == 0) {
+                const unsigned same = __match_any_sync(kFull, v);
+                const unsigned vmask = nvalid >= 32 ? kFull : ((1u << nvalid) - 1u);
+                first = valid && ((same & vmask & lanemask_lt()) == 0);
+            }
             uint8_t *srow = nullptr;
             if (staged) {
                 // copy the code row into shared memory now, so that it arrives during the visited check

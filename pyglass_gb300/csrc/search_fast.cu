@@ -1,6 +1,6 @@
 // The fast form of the batched search (search_core.cuh with NCH > 0) for the shapes the benchmark
 // workloads take: integer codes staged in shared memory as 64- or 128-byte rows, degree <= 32, visited
-// sets in the warps' global tables only and pools of at most 128 entries.  The search and its results
+// sets in the warps' global tables only and pools of at most 256 entries.  The search and its results
 // are those of the general form; the runtime tests it drops become compile-time facts, which cuts
 // the warp-instructions per expansion (on 1M x 128 SQ4U at ef 128: 1089 M -> 909 M per launch).
 // Compiled in its own translation unit so that it builds in parallel with the general launches.
@@ -53,7 +53,7 @@ bool search_fast_fits(const IndexView &ix, const LaunchCfg &cfg) {
     const bool int_kind = ix.kind == K_SQ4U || ix.kind == K_SQ8U || ix.kind == K_SQ2U || ix.kind == K_SQ4UA ||
                           ix.kind == K_SQ1;
     return int_kind && (cfg.L.stage_row == 64 || cfg.L.stage_row == 128) && ix.K <= 32 && cfg.L.table_bits == 0 &&
-           cfg.L.pool_cap <= 128;
+           cfg.L.pool_cap <= 256;
 }
 
 cudaError_t launch_search_fast(const IndexView &ix, const BatchView &bv, const LaunchCfg &cfg, cudaStream_t st) {
