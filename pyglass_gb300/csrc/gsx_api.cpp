@@ -237,13 +237,23 @@ int make_cfg(gsx_searcher *s, int kmax, int efmax, int nq, bool single, int tabl
 // seen on this searcher with 25% headroom (before any batch: half of ef*K), at the kernel's 7/8
 // load limit, then one size up so that buckets rarely fill, 2^11..2^20 slots.  A query that still
 // outgrows it is re-run by resolve_overflow.
-int spill_bits_for(const gsx_searcher *s, const LaunchCfg &cfg) {
-    if (s->tuning.spill_bits > 0) return s->tuning.spill_bits;
-    const int64_t want = s->visit_hint > 0 ? (int64_t)s->visit_hint * 5 / 4 + s->ix.K
-                                           : (int64_t)cfg.L.cap * s->ix.K / 2;
+// The automatic size also covers three quarters of (pool capacity x degree) visits, so that a launch
+// with a larger ef than any batch seen so far (a serving mix up to ef 256 after an ef-128 batch) does
+// not start on tables sized for the smaller pools.
+int auto_spill_bits(const gsx_searcher *s, const LaunchCfg &cfg) {
+    int64_t want = s->visit_hint > 0 ? (int64_t)s->visit_hint * 5 / 4 + s->ix.K : (int64_t)cfg.L.cap * s->ix.K / 2;
+    want = std::max<int64_t>(want, (int64_t)cfg.L.pool_cap * s->ix.K * 3 / 4);
     int bits = 10;
     while ((1ll << bits) - ((1ll << bits) >> 3) < want && bits < 19) ++bits;
     return bits + 1;
+}
+
+// A size set through set_tuning is used as given (a caller may want small tables); one picked by
+// optimize for the ef it ran at is raised to the automatic size of a launch with larger pools.
+int spill_bits_for(const gsx_searcher *s, const LaunchCfg &cfg) {
+    if (s->tuning.spill_bits > 0 && !s->spill_from_optimize) return s->tuning.spill_bits;
+    const int a = auto_spill_bits(s, cfg);
+    return s->tuning.spill_bits > a ? s->tuning.spill_bits : a;
 }
 
 // Direction of the batch order: the principal direction of the sampled base rows (power iteration
@@ -850,6 +860,7 @@ int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t) {
         if (t->spill_bits != 0 && (t->spill_bits < kMinTableBits || t->spill_bits > 20))
             return fail(GSX_ERR_INVALID, "spill_bits must be 0 or in [%d, 20]", kMinTableBits);
         s->tuning = *t;
+        s->spill_from_optimize = false;
         if (is_float_kind(s->kind) && s->tuning.lanes_per_row == 2) s->tuning.lanes_per_row = 4;
         return GSX_OK;
     } GSX_ABI_GUARD("gsx_searcher_set_tuning")
@@ -902,8 +913,7 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
             for (int lpr : lprs)
                 for (int bits : bit_choices)
                 for (int pf : pfs)
-                for (int sb : {auto_sb - 1, auto_sb, auto_sb + 1}) {
-                    if (sb < kMinTableBits) continue;
+                for (int sb : {auto_sb, auto_sb + 1}) {
                     gsx_tuning t{wpb, bits, lpr, pf, sb};
                     s->tuning = t;
                     float ms_min = 1e30f;
@@ -931,6 +941,7 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
                     }
                 }
         s->tuning = best;
+        s->spill_from_optimize = best.spill_bits > 0;
         return GSX_OK;
     } GSX_ABI_GUARD("gsx_searcher_optimize")
 }

@@ -133,5 +133,7 @@ struct gsx_searcher {
     int32_t sample_n = 0;
 
     gsx_tuning tuning{0, 0, 0, 0, 0};
+    bool spill_from_optimize = false;  // tuning.spill_bits was picked by optimize for its ef (a floor,
+                                       // not a cap: larger pools get the automatic size)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
