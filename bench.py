@@ -49,7 +49,10 @@ def args_():
     p.add_argument("--build-only", type=int, default=0, metavar="ROWS",
                    help="only the GPU NSG build of the first ROWS base rows (for ncu launch lists)")
     p.add_argument("--profile", action="store_true",
-                   help="only the warm-up and timed device launches (default tuning), for ncu captures")
+                   help="only the warm-up and timed device launches, for ncu captures (no autotuner run: the "
+                        "tuning is --tuning's, else the default)")
+    p.add_argument("--tuning", default=None, metavar="W,T,L,P,S",
+                   help="with --profile: warps per block, table bits, lanes per row, prefetch bits, spill bits")
     p.add_argument("--case", default=None, choices=sorted(CASES),
                    help="one small case of other kernels (for ncu captures): " + "; ".join(
                        f"{k}: {v[0]}" for k, v in sorted(CASES.items())))
@@ -448,6 +451,8 @@ def run_gpu(a):
     s.batch_search(queries, K)  # sizes the visited table from this workload's visit counts
     if not a.profile:
         s.optimize()
+    elif a.tuning:
+        s.set_tuning(*[int(x) for x in a.tuning.split(",")])
     tuning = s.get_tuning()
     # a stream of our own: the legacy default stream has handle 0, which the C ABI reads as
     # "the searcher's stream"
@@ -678,9 +683,9 @@ def _case_setdata():
 
     w = datasets.WORKLOADS[WORKLOAD]
     base, queries = w["base"](), w["queries"]()
-    g = glass.Graph(*graph_file())
     out = {}
     for quant, refine in (("SQ4U", "FP32"), ("SQ8U", ""), ("SQ8", ""), ("FP16", ""), ("E5M2", "")):
+        g = glass.Graph(*graph_file())  # a searcher takes its graph (the reference moves it in)
         torch.cuda.synchronize()
         t = time.perf_counter()
         s = glass.Searcher(g, base, "L2", quant, refine)

@@ -73,3 +73,16 @@ print("ok")
 """
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "ok" in r.stdout, r.stdout + r.stderr
+
+
+def test_profiling_cases_are_declared(monkeypatch):
+    """bench.py --case NAME runs one small case of the other kernels for ncu captures; every case
+    the help text names has a runner, and --tuning parses as five integers."""
+    import sys
+
+    assert {"setdata", "lowrank-e5m2", "lowrank-sq8u", "sphere-sq4u-ip"} <= set(bench.CASES)
+    for what, run in bench.CASES.values():
+        assert isinstance(what, str) and callable(run)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--profile", "--tuning", "2,1,1,2,13", "--case", "setdata"])
+    a = bench.args_()
+    assert a.case == "setdata" and [int(x) for x in a.tuning.split(",")] == [2, 1, 1, 2, 13]
