@@ -383,11 +383,11 @@ __device__ __forceinline__ void merge(WarpState &w, int &S, int cap, int &lb, in
     // enter, and its larger key does not change the rank of one that does
     const unsigned ltm = (1u << lane) - 1u;
     const uint32_t last = S == cap ? w.pkey[S - 1] : 0xffffffffu;
-    const bool v0 = lane < m, v1 = lane + 32 < m;
+    const bool v0 = lane < m, v1 = !SMALL && lane + 32 < m;
     const uint32_t k0 = v0 ? w.cand_key[lane] : 0u, k1 = v1 ? w.cand_key[lane + 32] : 0u;
     const int32_t i0 = v0 ? w.cand_id[lane] : 0, i1 = v1 ? w.cand_id[lane + 32] : 0;
     const bool s0 = v0 && (S < cap || k0 < last), s1 = v1 && (S < cap || k1 < last);
-    const unsigned b0 = __ballot_sync(kFull, s0), b1 = __ballot_sync(kFull, s1);
+    const unsigned b0 = __ballot_sync(kFull, s0), b1 = SMALL ? 0u : __ballot_sync(kFull, s1);
     const int ns = __popc(b0) + __popc(b1);
     if (ns == 0) {
         S = (S + m) < cap ? (S + m) : cap;
@@ -906,12 +906,13 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
 }
 
 // Resident 256-thread blocks per SM the register allocation is held to: 64 registers a thread for the
-// integer kinds, 64 for the 2-byte float rows and 80 for the other float kinds (measured on 1M x 128
-// at ef 128 against the unconstrained 128-register build: FP16 2.67 -> 2.11 ms, E5M2 2.69 -> 2.43 ms;
-// the few spilled words cost less than the resident warps they buy)
+// integer kinds and the 2-byte float rows (FP16 on 1M x 128 at ef 128: 2.67 ms with 128 registers,
+// 2.11 ms with 64 — the few spilled words cost less than the resident warps they buy), 128 for the
+// other float kinds (E5M2 on 1M x 960, where 1,000 queries fill less than one wave and the latency
+// of each query decides: 80 registers spill in the distance loop and took ef 64 from 578 k to 310 k QPS)
 template <int KIND>
 struct SearchMinBlocks {
-    static constexpr int value = IsIntKind<KIND>::value ? 4 : ((KIND == K_FP16 || KIND == K_BF16) ? 4 : 3);
+    static constexpr int value = IsIntKind<KIND>::value ? 4 : ((KIND == K_FP16 || KIND == K_BF16) ? 4 : 2);
 };
 
 template <int KIND, int METRIC, int LPR, int NCH = 0>
