@@ -464,6 +464,7 @@ int host_batch(gsx_searcher *s, const float *queries, int nq, int k, const int32
     }
     s->visit_hint = std::max(s->visit_hint, mx);
     if (nq >= 32) s->visit_avg = (double)sum / nq;
+    if (!single) s->last_batch_nq = nq;
     if (!single) {
         // SearchBatch: average distance computations (graph_searcher.hpp:156-158)
         int64_t tot = 0;
@@ -873,14 +874,19 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
         if (!s->has_data) return fail(GSX_ERR_STATE, "optimize before set_data");
         int rc = set_device(s);
         if (rc) return rc;
-        // the sample is tiled to enough queries to fill the GPU several times over, so that the timing
-        // measures throughput (a single wave would only measure the slowest query's latency)
-        const int reps = std::max(1, (16384 + s->sample_n - 1) / s->sample_n);
-        const int nq = s->sample_n * reps, k = 10, d = s->ix.d;
+        // the sample is tiled to the size of the last host batch (a batch smaller than one wave of
+        // resident warps is bound by its queries' latency, a larger one by throughput, and the best
+        // settings differ), or, before any batch, to enough queries to fill the GPU several times over
+        const int want = s->last_batch_nq > 0 ? std::min(std::max(s->last_batch_nq, 256), 65536) : 16384;
+        const int reps = std::max(1, (want + s->sample_n - 1) / s->sample_n);
+        const int nq = std::min(s->sample_n * reps, want), k = 10, d = s->ix.d;
         cudaStream_t st = s->stream;
         std::vector<float> tiled((size_t)nq * d);
-        for (int r = 0; r < reps; ++r)
-            std::memcpy(tiled.data() + (size_t)r * s->sample_n * d, s->sample.data(), (size_t)s->sample_n * d * 4);
+        for (int r = 0; r < reps; ++r) {
+            const int rows = std::min(s->sample_n, nq - r * s->sample_n);
+            if (rows > 0)
+                std::memcpy(tiled.data() + (size_t)r * s->sample_n * d, s->sample.data(), (size_t)rows * d * 4);
+        }
         if ((rc = upload(s->q, tiled.data(), (size_t)nq * d, st))) return rc;
         if ((rc = s->ids.ensure((size_t)nq * k * 4))) return rc;
         if ((rc = s->dis.ensure((size_t)nq * k * 4))) return rc;

@@ -127,6 +127,7 @@ struct gsx_searcher {
     double last_avg_cmps = 0.0;
     int32_t visit_hint = 0;  // largest per-query distance count seen
     double visit_avg = 0.0;  // mean per-query distance count of the last large batch
+    int32_t last_batch_nq = 0;  // queries of the last host batch (the size optimize tunes for)
 
     // sample of base rows kept for optimize (graph_searcher.hpp:62-69)
     std::vector<float> sample;
