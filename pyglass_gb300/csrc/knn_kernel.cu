@@ -35,6 +35,7 @@ constexpr int kTM = 128;          // queries per tile (MMA M)
 constexpr int kTN = 128;          // base rows per tile (MMA N)
 constexpr int kKB = 64;           // bf16 elements per 128-byte swizzled K block
 constexpr int kCand = 16;         // candidates kept per query per epilogue half per unit
+constexpr int kBuf = 32;          // candidates a thread may hold unmerged (exact inputs)
 constexpr int kEpiWarps = 8;
 constexpr int kThreads = 32 * (4 + kEpiWarps);
 constexpr uint32_t kTmemCols = 2 * kTN;  // two accumulators
@@ -135,6 +136,9 @@ struct __align__(1024) KnnSmem {
     __nv_bfloat16 x[2][2][2][kTN * kKB];       // [stage][hi, lo][K block]   (2 x 2 x 2 x 16 KB)
 };
 
+// the candidate buffers fit the low-half operand blocks of one stage each (values, then ids)
+static_assert(sizeof(float) * kBuf * kEpiWarps * 32 <= sizeof(__nv_bfloat16) * 2 * kTN * kKB,
+              "candidate buffer larger than a stage's low-half operand blocks");
 // dynamic shared memory carve-up (bytes): operands, then candidate lists, then barriers
 constexpr size_t kOpBytes = sizeof(KnnSmem);
 constexpr size_t kCandBytes = (size_t)kCand * kEpiWarps * 32 * 8;
@@ -260,6 +264,12 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
         const int half = ew >> 2;            // columns half*kTN/2 .. +kTN/2-1
         const int slot = ew * 32 + lane;     // this thread's candidate list
         const int row = quarter * 32 + lane; // query row within the tile
+        // with exact inputs (one pass) the low halves of the operand buffers are unused: they hold the
+        // per-thread candidate buffers (kBuf values and ids a thread, same stride as the lists)
+        const bool buffered = P.passes == 1;
+        float *bd = reinterpret_cast<float *>(S.x[0][1][0]);
+        int32_t *bi = reinterpret_cast<int32_t *>(S.x[1][1][0]);
+        int nb = 0;
         uint32_t it = 0;
         for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
             const int mt = u % P.n_mt, nc = u / P.n_mt;
@@ -299,6 +309,33 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                         m4[j & 3] = fminf(m4[j & 3], v[j]);
                     }
                     const float dmin = fminf(fminf(m4[0], m4[1]), fminf(m4[2], m4[3]));
+                    if (buffered) {
+                        // exact inputs: the values that beat this thread's threshold are appended to its
+                        // buffer (the threshold is only refreshed when the buffers merge), and the warp
+                        // merges every lane's buffer into its list at once when one could overflow, so
+                        // that no lane inserts alone while the other 31 wait
+                        if (!__any_sync(0xffffffffu, dmin < thr)) continue;
+                        int cnt = 0;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) cnt += v[j] < thr;
+                        if (__any_sync(0xffffffffu, nb + cnt > kBuf)) {
+                            for (int i = 0; i < nb; ++i) {
+                                const float dist = bd[i * kEpiWarps * 32 + slot];
+                                if (dist < thr) thr = cand_insert(cd, ci, slot, dist, bi[i * kEpiWarps * 32 + slot]);
+                            }
+                            nb = 0;
+                            __syncwarp();
+                        }
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (v[j] < thr) {
+                                bd[nb * kEpiWarps * 32 + slot] = v[j];
+                                bi[nb * kEpiWarps * 32 + slot] = n0 + j;
+                                ++nb;
+                            }
+                        }
+                        continue;
+                    }
                     if (!(dmin < thr)) continue;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
@@ -310,6 +347,13 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                 fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&tempty[ab]);
+            }
+            if (buffered) {  // the unit's last buffered values
+                for (int i = 0; i < nb; ++i) {
+                    const float dist = bd[i * kEpiWarps * 32 + slot];
+                    if (dist < thr) thr = cand_insert(cd, ci, slot, dist, bi[i * kEpiWarps * 32 + slot]);
+                }
+                nb = 0;
             }
             const int qi = mt * kTM + row;
             if (qi < P.nq) {
