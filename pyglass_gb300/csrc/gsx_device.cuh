@@ -305,6 +305,60 @@ __device__ __forceinline__ int32_t sq_partial_row(const uint4 *row, int nch, con
     }
 }
 
+// Partial integer distance of chunk c (16 bytes, of nch) of a code row held in registers, against
+// the query layout in shared memory: the same words sq_partial reads for that chunk.  Summed over the
+// chunks of a row in any split, the partials give sq_partial's exact integer.
+template <int KIND, int METRIC>
+__device__ __forceinline__ int32_t sq_partial_chunk(const uint4 v, int c, int nch, const uint32_t *qc) {
+    if (KIND == K_SQ4UA) {
+        const uint4 e = reinterpret_cast<const uint4 *>(qc)[c];
+        const uint4 o = reinterpret_cast<const uint4 *>(qc + 4 * nch)[c];
+        uint32_t aa = 0, ab = 0;
+        sq4a_word(v.x, e.x, o.x, aa, ab);
+        sq4a_word(v.y, e.y, o.y, aa, ab);
+        sq4a_word(v.z, e.z, o.z, aa, ab);
+        sq4a_word(v.w, e.w, o.w, aa, ab);
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (KIND == K_SQ1) {
+        const uint4 q = reinterpret_cast<const uint4 *>(qc)[c];
+        return __popc(v.x ^ q.x) + __popc(v.y ^ q.y) + __popc(v.z ^ q.z) + __popc(v.w ^ q.w);
+    } else if (KIND == K_SQ2U) {
+        const int nw = 4 * nch;
+        const uint32_t *q = qc + 4 * c;
+        uint32_t aa = 0, ab = 0;
+        sq2_word(v.x, q + 0, nw, aa, ab);
+        sq2_word(v.y, q + 1, nw, aa, ab);
+        sq2_word(v.z, q + 2, nw, aa, ab);
+        sq2_word(v.w, q + 3, nw, aa, ab);
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (KIND == K_SQ4U) {
+        const uint4 l = reinterpret_cast<const uint4 *>(qc)[c];
+        const uint4 h = reinterpret_cast<const uint4 *>(qc + 4 * nch)[c];
+        uint32_t aa = 0, ab = 0;
+        sq4_word(v.x, l.x, h.x, aa, ab);
+        sq4_word(v.y, l.y, h.y, aa, ab);
+        sq4_word(v.z, l.z, h.z, aa, ab);
+        sq4_word(v.w, l.w, h.w, aa, ab);
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else if (METRIC == M_L2) {
+        const uint4 q = reinterpret_cast<const uint4 *>(qc)[c];
+        uint32_t aa = 0, ab = 0;
+        aa = __dp4a(v.x, v.x, aa); ab = __dp4a(v.x, q.x, ab);
+        aa = __dp4a(v.y, v.y, aa); ab = __dp4a(v.y, q.y, ab);
+        aa = __dp4a(v.z, v.z, aa); ab = __dp4a(v.z, q.z, ab);
+        aa = __dp4a(v.w, v.w, aa); ab = __dp4a(v.w, q.w, ab);
+        return (int32_t)aa - 2 * (int32_t)ab;
+    } else {
+        const uint4 q = reinterpret_cast<const uint4 *>(qc)[c];
+        int32_t s = 0;
+        s = __dp4a((int)v.x, (int)q.x, s);
+        s = __dp4a((int)v.y, (int)q.y, s);
+        s = __dp4a((int)v.z, (int)q.z, s);
+        s = __dp4a((int)v.w, (int)q.w, s);
+        return s;
+    }
+}
+
 // Finishes a team's integer distance (all lanes of the warp must call it).
 template <int KIND, int METRIC, int LPR>
 __device__ __forceinline__ int32_t sq_finish(int32_t partial, int32_t qsq) {

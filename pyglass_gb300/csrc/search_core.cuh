@@ -147,6 +147,8 @@ struct WarpState {
     float *fq;
     uint32_t *qc;
     unsigned char *stage;        // staged code rows (one per lane)
+    int32_t *src;                // fast form: lane that staged fresh neighbour j of the row (acc_ub's
+                                 // words, free until the merge)
     int32_t *tab;                // shared-memory table (null when the query runs on the spill table)
     int tbits;
     uint32_t *spill;             // this warp's global table (tagged slots), or null
@@ -785,6 +787,33 @@ __device__ void search_one(const IndexView &ix, const BatchView &bv, const WarpL
             if (__any_sync(kFull, bad)) overflow = true;
             const unsigned nm = __ballot_sync(kFull, fresh);
             const int at = m + __popc(nm & lanemask_lt());
+            if constexpr (NCH > 0) {
+                // the fresh rows' distances by teams of four lanes: lane (team t, sub s) takes chunk s
+                // (and s + 4 when NCH is 8) of fresh row t of each pass of eight, reading the row where
+                // its own lane staged it (src), and the team's partials are summed by two shuffles;
+                // the integer arithmetic is exact, so the split changes no distance
+                const int cnt = __popc(nm);
+                if (fresh) w.src[at] = lane;
+                cp_async_wait_all();
+                __syncwarp();
+                const int team = lane >> 2, sub = lane & 3;
+                for (int b = 0; b < cnt; b += 8) {
+                    const int j = b + team;
+                    const int sj = w.src[j & 31] & 31;  // lanes past cnt read a stale, in-range slot
+                    const unsigned char *row = w.stage + sj * L.stage_stride;
+                    int32_t part = sq_partial_chunk<KIND, METRIC>(reinterpret_cast<const uint4 *>(row)[sub], sub, NCH, w.qc);
+                    if (NCH == 8)
+                        part += sq_partial_chunk<KIND, METRIC>(reinterpret_cast<const uint4 *>(row)[sub + 4], sub + 4, NCH,
+                                                               w.qc);
+                    const uint32_t key = key_of(sq_finish<KIND, METRIC, 4>(j < cnt ? part : 0, qsq));
+                    if (j < cnt && sub == 0) w.cand_key[j] = key;
+                }
+                if (fresh) w.cand_id[at] = v;
+                __syncwarp();  // the staged rows are read before the next expansion stages others
+                m += cnt;
+                if (endm) break;
+                continue;
+            }
             if (staged) {
                 // distance of this lane's own neighbour from the staged row (one lane per row)
                 cp_async_wait_all();
@@ -932,6 +961,7 @@ __global__ void __launch_bounds__(256, SearchMinBlocks<KIND>::value) search_kern
     w.fq = reinterpret_cast<float *>(ws + L.fq);
     w.qc = reinterpret_cast<uint32_t *>(ws + L.qc);
     w.stage = ws + L.stage;
+    w.src = w.acc_ub;
     const size_t slot = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     w.spill = bv.gtab ? bv.gtab + (slot << bv.gtab_bits) : nullptr;
     w.spill_epoch = bv.gtab ? bv.gtab_epoch + slot : nullptr;
