@@ -190,7 +190,10 @@ typedef struct {
                                  also prefetch that row's code rows; bit 5: also prefetch the
                                  visited-table buckets of that row's neighbours */
     int32_t spill_bits;       /* log2 of the slots of each warp's global visited table (4 bytes a
-                                 slot; 7..20, 0 = sized from the visit counts seen) */
+                                 slot; 7..20, 0 = sized from the visit counts seen).  A size that
+                                 gsx_searcher_optimize picked applies to launches whose automatic
+                                 size is at most the one it tuned against; others get the
+                                 automatic size. */
 } gsx_tuning;
 int gsx_searcher_get_tuning(const gsx_searcher *s, gsx_tuning *t);
 int gsx_searcher_set_tuning(gsx_searcher *s, const gsx_tuning *t);

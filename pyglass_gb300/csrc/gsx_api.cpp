@@ -248,11 +248,14 @@ int auto_spill_bits(const gsx_searcher *s, const LaunchCfg &cfg) {
     return bits + 1;
 }
 
-// A size set through set_tuning is used as given (a caller may want small tables); one picked by
-// optimize for the ef it ran at is raised to the automatic size of a launch with larger pools.
+// A size set through set_tuning is used as given (a caller may want small tables).  One picked by
+// optimize (from one size below the automatic size to one above) holds for launches whose automatic
+// size is at most the one it was tuned against; a launch with larger pools, or after larger visit
+// counts than optimize saw, gets at least the automatic size.
 int spill_bits_for(const gsx_searcher *s, const LaunchCfg &cfg) {
     if (s->tuning.spill_bits > 0 && !s->spill_from_optimize) return s->tuning.spill_bits;
     const int a = auto_spill_bits(s, cfg);
+    if (s->tuning.spill_bits > 0 && a <= s->spill_auto_at_opt) return s->tuning.spill_bits;
     return s->tuning.spill_bits > a ? s->tuning.spill_bits : a;
 }
 
@@ -899,6 +902,9 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
         std::vector<int> bit_choices{kGlobalOnly, 9};
         (void)base_bits;
         const int sb0 = s->tuning.spill_bits;
+        const bool sfo0 = s->spill_from_optimize;
+        const int sao0 = s->spill_auto_at_opt;
+        s->spill_from_optimize = false;  // the sweep's sizes are used as given
         s->tuning.spill_bits = 0;
         LaunchCfg probe;
         int auto_sb = 14;
@@ -919,7 +925,7 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
             for (int lpr : lprs)
                 for (int bits : bit_choices)
                 for (int pf : pfs)
-                for (int sb : {auto_sb, auto_sb + 1}) {
+                for (int sb : {auto_sb - 1, auto_sb, auto_sb + 1}) {
                     gsx_tuning t{wpb, bits, lpr, pf, sb};
                     s->tuning = t;
                     float ms_min = 1e30f;
@@ -934,6 +940,8 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
                         cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st);
                         if (cudaStreamSynchronize(st) != cudaSuccess) {
                             s->tuning = saved;
+                            s->spill_from_optimize = sfo0;
+                            s->spill_auto_at_opt = sao0;
                             return cuda_fail(cudaGetLastError(), "optimize");
                         }
                         if (nover) { ok = false; break; }  // a table that overflows is not a candidate
@@ -947,7 +955,13 @@ int gsx_searcher_optimize(gsx_searcher *s, int32_t num_threads) {
                     }
                 }
         s->tuning = best;
-        s->spill_from_optimize = best.spill_bits > 0;
+        if (best_ms < 1e30f) {
+            s->spill_from_optimize = best.spill_bits > 0;
+            s->spill_auto_at_opt = auto_sb;
+        } else {  // nothing ran: the saved tuning stands, with its own origin
+            s->spill_from_optimize = sfo0;
+            s->spill_auto_at_opt = sao0;
+        }
         return GSX_OK;
     } GSX_ABI_GUARD("gsx_searcher_optimize")
 }

@@ -134,7 +134,8 @@ struct gsx_searcher {
     int32_t sample_n = 0;
 
     gsx_tuning tuning{0, 0, 0, 0, 0};
-    bool spill_from_optimize = false;  // tuning.spill_bits was picked by optimize for its ef (a floor,
-                                       // not a cap: larger pools get the automatic size)
+    bool spill_from_optimize = false;  // tuning.spill_bits was picked by optimize for its ef (launches
+                                       // with larger pools get the automatic size)
+    int spill_auto_at_opt = 0;         // the automatic size when optimize picked it
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };

@@ -168,6 +168,21 @@ def test_optimize_keeps_results(gpu):
     b = s.batch_search(q, 10)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+    # a visited-table size optimize picked at ef 32 (it may be one below the automatic size) gives way
+    # to the automatic size of larger pools: the device batch, which re-runs nothing, answers every
+    # query at ef 256 as the host batch does
+    torch = pytest.importorskip("torch")
+    s.set_ef(256)
+    hi, hd = s.batch_search(q, 10)
+    dq = torch.from_numpy(q).cuda()
+    di = torch.empty((q.shape[0], 10), dtype=torch.int32, device="cuda")
+    dd = torch.empty((q.shape[0], 10), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    s.batch_search_device(dq.data_ptr(), q.shape[0], 10, di.data_ptr(), dd.data_ptr(), kmax=10)
+    torch.cuda.synchronize()
+    assert s.overflow_count() == 0
+    np.testing.assert_array_equal(di.cpu().numpy(), hi)
+    np.testing.assert_array_equal(dd.cpu().numpy(), hd)
     s.set_tuning(0, 0, 0, 2, 0)
 
 
