@@ -451,14 +451,21 @@ int host_batch(gsx_searcher *s, const float *queries, int nq, int k, const int32
     rc = enqueue(s, s->q.as<float>(), nq, k, s->ef, d_ef, d_k, kmax, efmax, s->ids.as<int32_t>(), s->dis.as<float>(),
                  s->cmps.as<int32_t>(), single, st);
     if (rc) return rc;
-    rc = resolve_overflow(s, s->q.as<float>(), nq, k, s->ef, d_ef, d_k, kmax, efmax, s->ids.as<int32_t>(),
-                          s->dis.as<float>(), s->cmps.as<int32_t>(), single, st);
-    if (rc) return rc;
-    GSX_CUDA(cudaMemcpyAsync(ids, s->ids.p, (size_t)nq * kmax * 4, cudaMemcpyDeviceToHost, st));
-    if (dis) GSX_CUDA(cudaMemcpyAsync(dis, s->dis.p, (size_t)nq * kmax * 4, cudaMemcpyDeviceToHost, st));
+    // the results and the overflow count come back together, with one wait; a batch in which a query
+    // overflowed its visited table (rare) re-runs those queries and copies the results again
     s->h_cmps.resize((size_t)nq);
-    GSX_CUDA(cudaMemcpyAsync(s->h_cmps.data(), s->cmps.p, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
-    GSX_CUDA(cudaStreamSynchronize(st));
+    unsigned nover = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        GSX_CUDA(cudaMemcpyAsync(ids, s->ids.p, (size_t)nq * kmax * 4, cudaMemcpyDeviceToHost, st));
+        if (dis) GSX_CUDA(cudaMemcpyAsync(dis, s->dis.p, (size_t)nq * kmax * 4, cudaMemcpyDeviceToHost, st));
+        GSX_CUDA(cudaMemcpyAsync(s->h_cmps.data(), s->cmps.p, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
+        if (pass == 0) GSX_CUDA(cudaMemcpyAsync(&nover, s->counters.as<unsigned>() + 1, 4, cudaMemcpyDeviceToHost, st));
+        GSX_CUDA(cudaStreamSynchronize(st));
+        if (pass == 1 || nover == 0) break;
+        rc = resolve_overflow(s, s->q.as<float>(), nq, k, s->ef, d_ef, d_k, kmax, efmax, s->ids.as<int32_t>(),
+                              s->dis.as<float>(), s->cmps.as<int32_t>(), single, st);
+        if (rc) return rc;
+    }
     int32_t mx = 0;
     int64_t sum = 0;
     for (int i = 0; i < nq; ++i) {
