@@ -1,8 +1,9 @@
 // The fast form of the batched search (search_core.cuh with NCH > 0) for the shapes the benchmark
 // workloads take: integer codes staged in shared memory as 64- or 128-byte rows, degree <= 32, visited
 // sets in the warps' global tables only and pools of at most 256 entries.  The search and its results
-// are those of the general form; the runtime tests it drops become compile-time facts, which cuts
-// the warp-instructions per expansion (on 1M x 128 SQ4U at ef 128: 1089 M -> 909 M per launch).
+// are those of the general form; the runtime tests it drops become compile-time facts, and the fresh
+// staged rows are scored by teams of four lanes, which cuts the warp-instructions per launch (on
+// 1M x 128 SQ4U at ef 128, 10,000 queries: 1089 M in the general form, 849 M here).
 // Compiled in its own translation unit so that it builds in parallel with the general launches.
 #include "search_core.cuh"
 
