@@ -11,7 +11,8 @@
 // Kernel layout (one CTA per SM, persistent over (query tile, base chunk) units):
 //   warp 0      TMA producer: query tile (128 x 128 bf16) and base tiles (128 x 128 bf16), 128-byte
 //               swizzled, two stages
-//   warp 1      TMEM allocation (256 columns = two 128x128 fp32 accumulators) and the MMA issuer
+//   warp 1      TMEM allocation (all 512 columns = four 128x128 fp32 accumulators, so that the
+//               tensor cores run up to four tiles ahead of the slowest epilogue warp) and the MMA issuer
 //               (one elected thread, tcgen05.mma kind::f16, M=128 N=128 K=16)
 //   warps 4-11  epilogue: tcgen05.ld of the accumulator (warp w reads TMEM lanes 32*(w%4).., half
 //               (w-4)/4 of the columns), distance = fma(neg_scale, score, bias) for 32 columns at a
@@ -38,7 +39,8 @@ constexpr int kCand = 16;         // candidates kept per query per epilogue half
 constexpr int kBuf = 32;          // candidates a thread may hold unmerged (exact inputs)
 constexpr int kEpiWarps = 8;
 constexpr int kThreads = 32 * (4 + kEpiWarps);
-constexpr uint32_t kTmemCols = 2 * kTN;  // two accumulators
+constexpr int kAcc = 4;           // accumulators in TMEM (one CTA per SM holds all 512 columns)
+constexpr uint32_t kTmemCols = kAcc * kTN;
 
 struct KnnParams {
     int nq, N, dp;                // dp = padded dimension (multiple of 64)
@@ -143,6 +145,10 @@ static_assert(sizeof(float) * kBuf * kEpiWarps * 32 <= sizeof(__nv_bfloat16) * 2
 constexpr size_t kOpBytes = sizeof(KnnSmem);
 constexpr size_t kCandBytes = (size_t)kCand * kEpiWarps * 32 * 8;
 constexpr size_t kSmemBytes = kOpBytes + kCandBytes + 256 + 1024;
+// the barrier area holds 4 + 2 * kAcc + 2 mbarriers and the TMEM address word
+static_assert((7 + 2 * kAcc) * 8 <= 256, "barrier area too small");
+// a second CTA on an SM would find no TMEM columns left: the shared memory admits one
+static_assert(kSmemBytes > 228 * 1024 / 2, "two CTAs per SM would contend for TMEM");
 
 // Inserts (dist, n) into this thread's ascending candidate list (stride kEpiWarps*32 in shared
 // memory), dropping the last entry; returns the new threshold (the last entry).  Kept out of line:
@@ -168,9 +174,9 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
     float *cd = reinterpret_cast<float *>(base + kOpBytes);
     int32_t *ci = reinterpret_cast<int32_t *>(base + kOpBytes + kCandBytes / 2);
     uint64_t *bars = reinterpret_cast<uint64_t *>(base + kOpBytes + kCandBytes);
-    uint64_t *full = bars, *empty = bars + 2, *tfull = bars + 4, *tempty = bars + 6, *qfull = bars + 8,
-             *qempty = bars + 9;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 12);
+    uint64_t *full = bars, *empty = bars + 2, *tfull = bars + 4, *tempty = bars + 4 + kAcc,
+             *qfull = bars + 4 + 2 * kAcc, *qempty = bars + 5 + 2 * kAcc;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 6 + 2 * kAcc);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int kblocks = P.dp / kKB;  // 2 for d <= 128
@@ -181,6 +187,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
         for (int i = 0; i < 2; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < kAcc; ++i) {
             mbar_init(&tfull[i], 1);
             mbar_init(&tempty[i], kEpiWarps);
         }
@@ -232,9 +240,9 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                 if (!mbar_wait(qfull, ut & 1)) { ok = false; break; }
                 const int t0 = nc * P.tiles_per_chunk, t1 = min(P.n_tiles, t0 + P.tiles_per_chunk);
                 for (int t = t0; t < t1; ++t, ++it) {
-                    const int st = it & 1, ab = it & 1;
+                    const int st = it & 1, ab = it % kAcc;
                     if (!mbar_wait(&full[st], (it >> 1) & 1)) { ok = false; break; }
-                    if (!mbar_wait(&tempty[ab], ((it >> 1) & 1) ^ 1)) { ok = false; break; }
+                    if (!mbar_wait(&tempty[ab], ((it / kAcc) & 1) ^ 1)) { ok = false; break; }
                     fence_after();
                     const uint32_t d = tmem + (uint32_t)(ab * kTN);
                     uint32_t acc = 0;
@@ -280,8 +288,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
             float thr = __int_as_float(0x7f800000);
             const int t0 = nc * P.tiles_per_chunk, t1 = min(P.n_tiles, t0 + P.tiles_per_chunk);
             for (int t = t0; t < t1; ++t, ++it) {
-                const int ab = it & 1;
-                if (!mbar_wait(&tfull[ab], (it >> 1) & 1)) { ok = false; break; }
+                const int ab = it % kAcc;
+                if (!mbar_wait(&tfull[ab], (it / kAcc) & 1)) { ok = false; break; }
                 fence_after();
                 for (int c = 0; c < kTN / 64; ++c) {
                     const int n0 = t * kTN + half * (kTN / 2) + c * 32;
