@@ -49,6 +49,8 @@ struct KnnParams {
     int ip;                       // 1 = inner product
     float neg_scale;              // -2 (L2) or -1 (IP): approximate distance = bias + neg_scale * score
     const float *bias;            // n_tiles*kTN: |x|^2 (L2) or 0 (IP) per base row, +inf past N
+    int *bound;                   // nq or null: order-preserving key of the smallest kCand-th approximate
+                                  // distance any finished unit found for the query (exact inputs, k <= kCand)
     int32_t *cand;                // nq x n_chunks x 2 x kCand ids (-1 = none)
     float *cand_d;                // matching approximate distances
     unsigned *error;              // set on a timed-out wait
@@ -153,6 +155,13 @@ static_assert(kSmemBytes > 228 * 1024 / 2, "two CTAs per SM would contend for TM
 // Inserts (dist, n) into this thread's ascending candidate list (stride kEpiWarps*32 in shared
 // memory), dropping the last entry; returns the new threshold (the last entry).  Kept out of line:
 // its 32 call sites in the unrolled epilogue would otherwise swamp the instruction cache.
+// Order-preserving int key of a float (no NaN): keys compare as the floats do.
+__device__ __forceinline__ int fkey(float f) {
+    const int b = __float_as_int(f);
+    return b >= 0 ? b : b ^ 0x7fffffff;
+}
+__device__ __forceinline__ float fkey_inv(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+
 __device__ __noinline__ float cand_insert(float *cd, int32_t *ci, int slot, float dist, int n) {
     int pos = kCand - 1;
     while (pos > 0 && cd[(pos - 1) * kEpiWarps * 32 + slot] > dist) {
@@ -285,7 +294,18 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                 cd[c * kEpiWarps * 32 + slot] = __int_as_float(0x7f800000);
                 ci[c * kEpiWarps * 32 + slot] = -1;
             }
-            float thr = __int_as_float(0x7f800000);
+            // the threshold starts at the best bound other units have published for the query, raised
+            // by one ulp so that rows equal to it still enter (ties are ranked by id later), and never
+            // rises above it: a full list of kCand rows at or below a value bounds the query's kCand-th
+            // nearest, so no row above it can be among the top k <= kCand
+            const int qs = mt * kTM + row;
+            float cap = __int_as_float(0x7f800000);
+            if (P.bound && qs < P.nq) {
+                const int bk = *reinterpret_cast<volatile const int *>(P.bound + qs);
+                const float bf = fkey_inv(bk);
+                if (bf < __int_as_float(0x7f800000)) cap = nextafterf(bf, __int_as_float(0x7f800000));
+            }
+            float thr = cap;
             const int t0 = nc * P.tiles_per_chunk, t1 = min(P.n_tiles, t0 + P.tiles_per_chunk);
             for (int t = t0; t < t1; ++t, ++it) {
                 const int ab = it % kAcc;
@@ -329,7 +349,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                         if (__any_sync(0xffffffffu, nb + cnt > kBuf)) {
                             for (int i = 0; i < nb; ++i) {
                                 const float dist = bd[i * kEpiWarps * 32 + slot];
-                                if (dist < thr) thr = cand_insert(cd, ci, slot, dist, bi[i * kEpiWarps * 32 + slot]);
+                                if (dist < thr)
+                                    thr = fminf(cap, cand_insert(cd, ci, slot, dist, bi[i * kEpiWarps * 32 + slot]));
                             }
                             nb = 0;
                             __syncwarp();
@@ -349,7 +370,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
                     for (int j = 0; j < 32; ++j) {
                         const int n = n0 + j;
                         const float dist = v[j];
-                        if (dist < thr) thr = cand_insert(cd, ci, slot, dist, n);
+                        if (dist < thr) thr = fminf(cap, cand_insert(cd, ci, slot, dist, n));
                     }
                 }
                 fence_before();
@@ -359,11 +380,16 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tq_hi, const __grid_constant__
             if (buffered) {  // the unit's last buffered values
                 for (int i = 0; i < nb; ++i) {
                     const float dist = bd[i * kEpiWarps * 32 + slot];
-                    if (dist < thr) thr = cand_insert(cd, ci, slot, dist, bi[i * kEpiWarps * 32 + slot]);
+                    if (dist < thr) thr = fminf(cap, cand_insert(cd, ci, slot, dist, bi[i * kEpiWarps * 32 + slot]));
                 }
                 nb = 0;
             }
             const int qi = mt * kTM + row;
+            if (P.bound && qi < P.nq && ok) {
+                // a full list publishes its last entry as a bound for the query's later units
+                const float last = cd[(kCand - 1) * kEpiWarps * 32 + slot];
+                if (last < __int_as_float(0x7f800000)) atomicMin(P.bound + qi, fkey(last));
+            }
             if (qi < P.nq) {
                 const size_t o = (((size_t)qi * P.n_chunks + nc) * 2 + half) * kCand;
                 for (int c = 0; c < kCand; ++c) {
@@ -662,7 +688,7 @@ int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries
     if (d > 128) return fail(GSX_ERR_UNSUPPORTED, "exact kNN supports d <= 128");
     if (N > (int64_t)INT32_MAX) return fail(GSX_ERR_INVALID, "N too large");
     const int dp = 128;  // two 64-element K blocks
-    DevBuf xh, xl, qh, ql, xn, bias, cand, cand_d, cnt;
+    DevBuf xh, xl, qh, ql, xn, bias, cand, cand_d, cnt, bnd;
     int rc;
     if ((rc = xh.ensure((size_t)N * dp * 2)) || (rc = xl.ensure((size_t)N * dp * 2)) ||
         (rc = qh.ensure((size_t)nq * dp * 2)) || (rc = ql.ensure((size_t)nq * dp * 2)) || (rc = xn.ensure((size_t)N * 4)) ||
@@ -705,6 +731,13 @@ int knn_select(const float *d_base, int64_t N, int32_t d, const float *d_queries
     P.cand = cand.as<int32_t>();
     P.cand_d = cand_d.as<float>();
     P.error = cnt.as<unsigned>() + 1;
+    // exact inputs and k <= kCand without rechecks (the ground truth): units share per-query bounds
+    P.bound = nullptr;
+    if (P.passes == 1 && !fp32_l2 && self_base < 0 && k <= kCand) {
+        if ((rc = bnd.ensure((size_t)nq * 4))) return rc;
+        GSX_CUDA(cudaMemsetAsync(bnd.p, 0x7f, (size_t)nq * 4, st));  // key 0x7f7f7f7f: 3.4e38, above every distance
+        P.bound = bnd.as<int>();
+    }
     CUtensorMap mqh, mql, mxh, mxl;
     if ((rc = encode_map(&mqh, qh.p, nq, dp, kTM)) || (rc = encode_map(&mql, ql.p, nq, dp, kTM)) ||
         (rc = encode_map(&mxh, xh.p, N, dp, kTN)) || (rc = encode_map(&mxl, xl.p, N, dp, kTN)))
